@@ -1,0 +1,163 @@
+/*
+ * libdwt_gb300 -- GB300 (sm_103a) drop-in for the lifting-scheme wavelet hot
+ * path of libdwt (slchen/libdwt, VERSION 2013-01-29-dev).
+ *
+ * The first group of declarations is libdwt's own C API for the path, with
+ * the same names, argument meaning, memory model (byte strides, in place,
+ * outer/inner frame) and error behaviour (log, then abort).  Each one cites
+ * the reference declaration it replaces.  Pointers may be host memory
+ * (pageable or pinned) or device/managed memory of the current device; every
+ * call is synchronous on return, like the reference.
+ *
+ * The second group (dwt_gpu_*) is this library's extension: non-aborting
+ * variants that return an error code, device-resident out-of-place forms with
+ * an explicit stream, the batched strided 1D form, the batched 2D form and
+ * the serving loop.
+ */
+#ifndef LIBDWT_GB300_H
+#define LIBDWT_GB300_H
+
+#if defined(__GNUC__)
+#define DWT_EXPORT __attribute__((visibility("default")))
+#else
+#define DWT_EXPORT
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ 2D, float */
+
+/* src/libdwt.h:491-502 (src/libdwt.c:6286-6408): in-place forward CDF 9/7,
+ * *j_max_ptr levels (clamped to the limit and written back). */
+DWT_EXPORT void dwt_cdf97_2f_s(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                    int size_i_big_x, int size_i_big_y, int *j_max_ptr, int decompose_one,
+                    int zero_padding);
+
+/* src/libdwt.h:509-520 (src/libdwt.c:6410-6491): in-place forward CDF 5/3. */
+DWT_EXPORT void dwt_cdf53_2f_s(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                    int size_i_big_x, int size_i_big_y, int *j_max_ptr, int decompose_one,
+                    int zero_padding);
+
+/* src/libdwt.h:563-574 (src/libdwt.c:6647-6755): in-place inverse CDF 9/7. */
+DWT_EXPORT void dwt_cdf97_2i_s(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                    int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                    int zero_padding);
+
+/* src/libdwt.h:581-592 (src/libdwt.c:6757-6832): in-place inverse CDF 5/3. */
+DWT_EXPORT void dwt_cdf53_2i_s(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                    int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                    int zero_padding);
+
+/* ------------------------------------------------------------------ 1D, float */
+
+/* src/libdwt.h:219-226 (src/libdwt.c:5512-5557): one forward CDF 9/7 level of
+ * N samples `stride` bytes apart; L to dst_l, H to dst_h (same stride).
+ * tmp is accepted and not used. */
+DWT_EXPORT void dwt_cdf97_f_ex_stride_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N,
+                             int stride);
+
+/* src/libdwt.h:327-334 (src/libdwt.c:5779-5824): one inverse CDF 9/7 level. */
+DWT_EXPORT void dwt_cdf97_i_ex_stride_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N,
+                             int stride);
+
+/* src/libdwt.h:233-240 (src/libdwt.c:5559-5603): one forward CDF 5/3 level. */
+DWT_EXPORT void dwt_cdf53_f_ex_stride_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N,
+                             int stride);
+
+/* src/libdwt.h:341-348 (src/libdwt.c:5826-5870): one inverse CDF 5/3 level. */
+DWT_EXPORT void dwt_cdf53_i_ex_stride_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N,
+                             int stride);
+
+/* src/libdwt.h:165-184, 273-292 (src/libdwt.c:1433-1465, 5639-5671): the
+ * contiguous forms, stride = sizeof(float). */
+DWT_EXPORT void dwt_cdf97_f_ex_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N);
+DWT_EXPORT void dwt_cdf53_f_ex_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N);
+DWT_EXPORT void dwt_cdf97_i_ex_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N);
+DWT_EXPORT void dwt_cdf53_i_ex_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N);
+
+/* src/libdwt.h:57-134 (src/libdwt.c:1309-1337, 1369-1397): the deprecated
+ * forms with L and H concatenated in one array. */
+DWT_EXPORT void dwt_cdf97_f_s(const float *src, float *dst, float *tmp, int N);
+DWT_EXPORT void dwt_cdf53_f_s(const float *src, float *dst, float *tmp, int N);
+DWT_EXPORT void dwt_cdf97_i_s(const float *src, float *dst, float *tmp, int N);
+DWT_EXPORT void dwt_cdf53_i_s(const float *src, float *dst, float *tmp, int N);
+
+/* ----------------------------------------------------------------- lifecycle */
+
+/* src/libdwt.h:851 (src/libdwt.c:7466-7490): bring up the GPU context, the
+ * working stream and the buffer pool (also done lazily by the first call). */
+DWT_EXPORT void dwt_util_init(void);
+
+/* src/libdwt.h:856 (src/libdwt.c:7492-7510): release the pool and stream. */
+DWT_EXPORT void dwt_util_finish(void);
+
+/* src/libdwt.h:845 (src/libdwt.c:7668-7672): selects a CPU lifting kernel in
+ * the reference; recorded and ignored here (every value computes the same
+ * bits on the GPU). */
+DWT_EXPORT void dwt_util_set_accel(int accel_type);
+
+/* src/libdwt.h:606-618 (src/libdwt.c:624-634). */
+DWT_EXPORT int dwt_util_ceil_log2(int x);
+DWT_EXPORT int dwt_util_pow2_ceil_log2(int x);
+
+/* ------------------------------------------------------------- extensions */
+
+/* Error codes of the dwt_gpu_* functions (0 = success). */
+#define DWT_GPU_OK 0
+#define DWT_GPU_EINVAL (-1)      /* invalid arguments */
+#define DWT_GPU_ECUDA (-2)       /* a CUDA call failed */
+#define DWT_GPU_ENOMEM (-3)      /* device memory exhausted */
+#define DWT_GPU_EDEVICE (-4)     /* a device-side wait gave up (error word set) */
+#define DWT_GPU_EBUSY (-5)       /* admission refused (serving budget) */
+#define DWT_GPU_ENOTFOUND (-6)   /* unknown request id */
+
+/* Wavelet / direction selectors of the extension API. */
+#define DWT_GPU_CDF97 0
+#define DWT_GPU_CDF53 1
+
+/* Last error of this thread (0 if none) and its text. */
+DWT_EXPORT int dwt_gpu_get_last_error(void);
+DWT_EXPORT const char *dwt_gpu_error_string(int code);
+
+/* Non-aborting forms of the four 2D drop-ins: same arguments, wavelet and
+ * direction as parameters, return an error code. */
+DWT_EXPORT int dwt_gpu_2f_s(int wavelet, void *ptr, int stride_x, int stride_y, int size_o_big_x,
+                 int size_o_big_y, int size_i_big_x, int size_i_big_y, int *j_max_ptr,
+                 int decompose_one, int zero_padding);
+DWT_EXPORT int dwt_gpu_2i_s(int wavelet, void *ptr, int stride_x, int stride_y, int size_o_big_x,
+                 int size_o_big_y, int size_i_big_x, int size_i_big_y, int j_max,
+                 int decompose_one, int zero_padding);
+
+/* Non-aborting strided 1D level.  Forward (inverse = 0): a = src, b unused,
+ * c_or_l = dst_l, h_or_null = dst_h.  Inverse (inverse = 1): a = src_l,
+ * b = src_h, c_or_l = dst, h_or_null unused. */
+DWT_EXPORT int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float *c_or_l,
+                float *h_or_null, int N, int stride);
+
+/* Device-resident, out-of-place, asynchronous dense 2D transform of a w x h
+ * image (outer == inner): src and dst are device pointers with row pitches in
+ * bytes; src rows must be 16-byte aligned (pitch a multiple of 16, base
+ * 16-byte aligned).  The result is the reference's in-place layout written to
+ * dst.  j_levels < 0 means the full depth; the achieved depth is returned
+ * (>= 0) or an error code (< 0).  stream is a cudaStream_t (0 = default).
+ * Work is enqueued; the call does not synchronize. */
+DWT_EXPORT int dwt_gpu_2_dev(int wavelet, int inverse, const float *src, long long src_pitch_bytes,
+                  float *dst, long long dst_pitch_bytes, int w, int h, int j_levels,
+                  int decompose_one, void *stream);
+
+/* Batched strided 1D level, in place, device or host memory: `count`
+ * signals of N samples, signal s at base + (s / group) * group_stride +
+ * (s % group) * lane_stride bytes, samples `stride` bytes apart; L to samples
+ * [0, ceil(N/2)), H to [ceil(N/2), N) of each signal (the layout of a caller
+ * running dwt_cdf97_f_ex_stride_s with dst_l = src, dst_h = src +
+ * ceil(N/2)*stride on every signal).  One launch for the whole bank. */
+DWT_EXPORT int dwt_gpu_1_batch_s(int wavelet, int inverse, void *base, int N, int stride, long long count,
+                      int group, long long group_stride, int lane_stride);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBDWT_GB300_H */

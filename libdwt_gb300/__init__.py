@@ -1,0 +1,188 @@
+"""libdwt_gb300: GB300-native drop-in for libdwt's lifting wavelet hot path.
+
+The product is the C-ABI shared library ``libdwt_gb300/_lib/libdwt_gb300.so``
+(declared in ``include/libdwt.h``).  This module loads it with ctypes and
+mirrors the reference's C interface for Python callers: the same function
+names and arguments (raw addresses, byte strides, outer/inner frame, j_max,
+decompose_one, zero_padding), plus helpers that accept numpy arrays (host
+memory) and torch CUDA tensors (device memory).
+
+There is no CPU implementation here: if the library is missing, loading
+fails with an error naming the build step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .buildext import LIB, build, up_to_date  # noqa: F401
+
+__all__ = ["lib", "build", "CDF97", "CDF53", "DwtError", "transform2", "transform2_dev",
+           "strided_1d", "batch_1d"]
+
+CDF97 = 0
+CDF53 = 1
+_WAVELETS = {"cdf97": CDF97, "cdf53": CDF53, CDF97: CDF97, CDF53: CDF53}
+
+_vp = C.c_void_p
+_i = C.c_int
+_ll = C.c_longlong
+
+
+class DwtError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """The loaded CUDA library.  Raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise ImportError(f"libdwt_gb300 CUDA library not built ({LIB}); "
+                              "run python -c 'import __graft_entry__ as g; g.build()'")
+        L = C.CDLL(LIB)
+        for w in ("cdf97", "cdf53"):
+            getattr(L, f"dwt_{w}_2f_s").argtypes = [_vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
+            getattr(L, f"dwt_{w}_2i_s").argtypes = [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
+            getattr(L, f"dwt_{w}_f_ex_stride_s").argtypes = [_vp, _vp, _vp, _vp, _i, _i]
+            getattr(L, f"dwt_{w}_i_ex_stride_s").argtypes = [_vp, _vp, _vp, _vp, _i, _i]
+        L.dwt_gpu_2f_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
+        L.dwt_gpu_2i_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
+        L.dwt_gpu_1_s.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
+        L.dwt_gpu_2_dev.argtypes = [_i, _i, _vp, _ll, _vp, _ll, _i, _i, _i, _i, _vp]
+        L.dwt_gpu_1_batch_s.argtypes = [_i, _i, _vp, _i, _i, _ll, _i, _ll, _i]
+        L.dwt_gpu_error_string.restype = C.c_char_p
+        L.dwt_gpu_error_string.argtypes = [_i]
+        L.dwt_util_set_accel.argtypes = [_i]
+        L.dwt_util_ceil_log2.argtypes = [_i]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> int:
+    if rc < 0:
+        raise DwtError(lib().dwt_gpu_error_string(rc).decode())
+    return rc
+
+
+def _addr(x) -> int:
+    """Address of a numpy array, a torch tensor or an int."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+# ------------------------------------------------------------ reference API
+
+def dwt_cdf97_2f_s(ptr, stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+                   size_i_big_y, j_max, decompose_one=0, zero_padding=0) -> int:
+    """In-place forward CDF 9/7 (src/libdwt.c:6286).  Returns the achieved j_max."""
+    j = C.c_int(j_max)
+    _check(lib().dwt_gpu_2f_s(CDF97, _addr(ptr), stride_x, stride_y, size_o_big_x, size_o_big_y,
+                              size_i_big_x, size_i_big_y, C.byref(j), decompose_one, zero_padding))
+    return j.value
+
+
+def dwt_cdf53_2f_s(ptr, stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+                   size_i_big_y, j_max, decompose_one=0, zero_padding=0) -> int:
+    """In-place forward CDF 5/3 (src/libdwt.c:6410).  Returns the achieved j_max."""
+    j = C.c_int(j_max)
+    _check(lib().dwt_gpu_2f_s(CDF53, _addr(ptr), stride_x, stride_y, size_o_big_x, size_o_big_y,
+                              size_i_big_x, size_i_big_y, C.byref(j), decompose_one, zero_padding))
+    return j.value
+
+
+def dwt_cdf97_2i_s(ptr, stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+                   size_i_big_y, j_max, decompose_one=0, zero_padding=0) -> None:
+    """In-place inverse CDF 9/7 (src/libdwt.c:6647)."""
+    _check(lib().dwt_gpu_2i_s(CDF97, _addr(ptr), stride_x, stride_y, size_o_big_x, size_o_big_y,
+                              size_i_big_x, size_i_big_y, j_max, decompose_one, zero_padding))
+
+
+def dwt_cdf53_2i_s(ptr, stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+                   size_i_big_y, j_max, decompose_one=0, zero_padding=0) -> None:
+    """In-place inverse CDF 5/3 (src/libdwt.c:6757)."""
+    _check(lib().dwt_gpu_2i_s(CDF53, _addr(ptr), stride_x, stride_y, size_o_big_x, size_o_big_y,
+                              size_i_big_x, size_i_big_y, j_max, decompose_one, zero_padding))
+
+
+def dwt_cdf97_f_ex_stride_s(src, dst_l, dst_h, tmp, N, stride) -> None:
+    """Forward CDF 9/7 level of a strided signal (src/libdwt.c:5512)."""
+    _check(lib().dwt_gpu_1_s(CDF97, 0, _addr(src), None, _addr(dst_l), _addr(dst_h), N, stride))
+
+
+def dwt_cdf97_i_ex_stride_s(src_l, src_h, dst, tmp, N, stride) -> None:
+    """Inverse CDF 9/7 level of a strided signal (src/libdwt.c:5779)."""
+    _check(lib().dwt_gpu_1_s(CDF97, 1, _addr(src_l), _addr(src_h), _addr(dst), None, N, stride))
+
+
+def dwt_cdf53_f_ex_stride_s(src, dst_l, dst_h, tmp, N, stride) -> None:
+    """Forward CDF 5/3 level of a strided signal (src/libdwt.c:5559)."""
+    _check(lib().dwt_gpu_1_s(CDF53, 0, _addr(src), None, _addr(dst_l), _addr(dst_h), N, stride))
+
+
+def dwt_cdf53_i_ex_stride_s(src_l, src_h, dst, tmp, N, stride) -> None:
+    """Inverse CDF 5/3 level of a strided signal (src/libdwt.c:5826)."""
+    _check(lib().dwt_gpu_1_s(CDF53, 1, _addr(src_l), _addr(src_h), _addr(dst), None, N, stride))
+
+
+def dwt_util_init() -> None:
+    lib().dwt_util_init()
+
+
+def dwt_util_finish() -> None:
+    lib().dwt_util_finish()
+
+
+def dwt_util_set_accel(accel_type: int) -> None:
+    lib().dwt_util_set_accel(accel_type)
+
+
+# ------------------------------------------------------------ conveniences
+
+def transform2(buf, wavelet, direction: str, stride_x: int, stride_y: int, size_o, size_i,
+               j_max: int, decompose_one: int = 0, zero_padding: int = 0) -> int:
+    """One in-place 2D transform on a buffer (numpy array = host, torch CUDA
+    tensor = device) holding the frame at byte strides.  Returns the achieved
+    levels (forward) or the j_max argument (inverse)."""
+    w = _WAVELETS[wavelet]
+    ox, oy = size_o
+    ix, iy = size_i
+    if direction == "f":
+        j = C.c_int(j_max)
+        _check(lib().dwt_gpu_2f_s(w, _addr(buf), stride_x, stride_y, ox, oy, ix, iy, C.byref(j),
+                                  decompose_one, zero_padding))
+        return j.value
+    _check(lib().dwt_gpu_2i_s(w, _addr(buf), stride_x, stride_y, ox, oy, ix, iy, j_max,
+                              decompose_one, zero_padding))
+    return j_max
+
+
+def transform2_dev(src, dst, wavelet, inverse: bool, j_levels: int = -1, decompose_one: int = 0,
+                   stream: int = 0) -> int:
+    """Device-resident out-of-place dense transform of torch CUDA tensors
+    src -> dst (2D float32, row pitch = stride(0)).  Asynchronous on `stream`
+    (a raw cudaStream_t, 0 = default).  Returns the achieved depth."""
+    h, w = src.shape
+    return _check(lib().dwt_gpu_2_dev(_WAVELETS[wavelet], 1 if inverse else 0, src.data_ptr(),
+                                      src.stride(0) * 4, dst.data_ptr(), dst.stride(0) * 4, w, h,
+                                      j_levels, decompose_one, stream))
+
+
+def strided_1d(wavelet, inverse: bool, a, b, c, d, N: int, stride: int) -> None:
+    """Non-aborting strided 1D level on raw addresses / arrays / tensors."""
+    _check(lib().dwt_gpu_1_s(_WAVELETS[wavelet], 1 if inverse else 0, _addr(a),
+                             None if b is None else _addr(b), _addr(c),
+                             None if d is None else _addr(d), N, stride))
+
+
+def batch_1d(wavelet, inverse: bool, base, N: int, stride: int, count: int, group: int,
+             group_stride: int, lane_stride: int) -> None:
+    """Batched in-place strided 1D level over a bank of signals."""
+    _check(lib().dwt_gpu_1_batch_s(_WAVELETS[wavelet], 1 if inverse else 0, _addr(base), N, stride,
+                                   count, group, group_stride, lane_stride))

@@ -1,0 +1,722 @@
+// C-ABI of libdwt_gb300: libdwt's own entry points for the lifting hot path
+// (src/libdwt.h) plus the dwt_gpu_* extensions, over one GPU context.
+//
+// Every 2D call runs the same device pipeline:
+//   1. stage the caller's frame into a compact device frame IN whose rows are
+//      16-byte aligned (cudaMemcpy2DAsync for host memory with 4-byte pixels,
+//      a byte-gather kernel for anything else);
+//   2. transform IN -> OUT out of place, one fused level kernel per level,
+//      coarser LL bands ping-ponging between two compact scratch frames;
+//   3. write OUT back in the caller's layout (or have the level kernels write
+//      straight into a dense device caller frame).
+// Out of place is what makes the fused kernel legal: the reference works in
+// place, where one tile's outputs land on other tiles' inputs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/libdwt.h"
+#include "dwt_capi_internal.h"
+#include "dwt_generic.cuh"
+#include "dwt_level2d.cuh"
+
+namespace dwt {
+
+// ---------------------------------------------------------------- context
+
+static std::mutex g_init_mu;
+static Context *g_ctx = nullptr;
+static std::atomic<int> g_accel{0};
+static thread_local int t_last_error = DWT_GPU_OK;
+
+void log_error(const char *fmt, ...)
+{
+    // the reference's LOG_ERR format (src/libdwt.c:7953-7985)
+    flockfile(stderr);
+    fputs("ERROR: ", stderr);
+    va_list ap;
+    va_start(ap, fmt);
+    vfprintf(stderr, fmt, ap);
+    va_end(ap);
+    fflush(stderr);
+    funlockfile(stderr);
+}
+
+int set_error(int code)
+{
+    t_last_error = code;
+    return code;
+}
+
+Context &ctx()
+{
+    std::lock_guard<std::mutex> g(g_init_mu);
+    if (!g_ctx) {
+        Context *c = new Context();
+        const char *dev = getenv("DWT_GPU_DEVICE");
+        c->device = dev ? atoi(dev) : 0;
+        cudaSetDevice(c->device);
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        cudaMalloc(&c->d_err, sizeof(int));
+        cudaMemset(c->d_err, 0, sizeof(int));
+        cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+        g_ctx = c;
+    }
+    cudaSetDevice(g_ctx->device);
+    return *g_ctx;
+}
+
+void ctx_finish()
+{
+    std::lock_guard<std::mutex> g(g_init_mu);
+    if (!g_ctx) return;
+    cudaStreamSynchronize(g_ctx->stream);
+    g_ctx->pool.release_all();
+    cudaFree(g_ctx->d_err);
+    cudaStreamDestroy(g_ctx->stream);
+    delete g_ctx;
+    g_ctx = nullptr;
+}
+
+// ------------------------------------------------------------ helpers
+
+int ceil_log2_int(int x)
+{
+    int r = 0;
+    while ((1LL << r) < (long long)x) r++;
+    return r;
+}
+
+MemKind classify(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return MemKind::Pageable;
+    }
+    switch (a.type) {
+    case cudaMemoryTypeDevice: return MemKind::Device;
+    case cudaMemoryTypeManaged: return MemKind::Managed;
+    case cudaMemoryTypeHost: return MemKind::Pinned;
+    default: return MemKind::Pageable;
+    }
+}
+
+static long long align_up(long long v, long long a) { return (v + a - 1) / a * a; }
+
+// Scoped pool allocation on the context stream.
+struct Buf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    Buf() = default;
+    Buf(size_t bytes, cudaStream_t st) { alloc(bytes, st); }
+    bool alloc(size_t bytes, cudaStream_t st)
+    {
+        s = st;
+        p = ctx().pool.alloc(bytes, st);
+        return p != nullptr;
+    }
+    ~Buf()
+    {
+        if (p) ctx().pool.release(p, s);
+    }
+    Buf(const Buf &) = delete;
+    Buf &operator=(const Buf &) = delete;
+    float *f() const { return static_cast<float *>(p); }
+};
+
+#define CK(x)                                                                  \
+    do {                                                                       \
+        cudaError_t e_ = (x);                                                  \
+        if (e_ != cudaSuccess) {                                               \
+            log_error("CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return set_error(e_ == cudaErrorMemoryAllocation ? DWT_GPU_ENOMEM : DWT_GPU_ECUDA); \
+        }                                                                      \
+    } while (0)
+
+// Reads and clears the device error word after the stream drained.
+static int check_device_error(Context &c)
+{
+    int h = 0;
+    if (cudaMemcpy(&h, c.d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DWT_GPU_ECUDA;
+    if (h) {
+        cudaMemset(c.d_err, 0, sizeof(int));
+        log_error("device-side wait gave up (code %d)\n", h);
+        return DWT_GPU_EDEVICE;
+    }
+    return DWT_GPU_OK;
+}
+
+// ------------------------------------------------------- level pipelines
+
+size_t dense_scratch_floats(int W, int H, int J, long long *pitch0, long long *pitch1)
+{
+    const int w1 = (W + 1) / 2, h1 = (H + 1) / 2, w2 = (W + 3) / 4, h2 = (H + 3) / 4;
+    *pitch0 = align_up(w1, 32);
+    *pitch1 = align_up(w2, 32);
+    size_t n = 0;
+    if (J >= 2) n += size_t(*pitch0) * h1 + 64;
+    if (J >= 3) n += size_t(*pitch1) * h2 + 64;
+    return n;
+}
+
+cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long long out_pitch, int W,
+                          int H, int J, int wavelet, float *scratch, cudaStream_t s, int *err,
+                          int seg_hint)
+{
+    long long p[2];
+    dense_scratch_floats(W, H, J, &p[0], &p[1]);
+    float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
+    for (int j = 0; j < J; ++j) {
+        const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
+        const int wd = (w + 1) / 2, hd = (h + 1) / 2;
+        LevelDesc d{};
+        d.w = w;
+        d.h = h;
+        d.in[0] = j == 0 ? in : buf[(j - 1) % 2];
+        d.in_pitch[0] = j == 0 ? in_pitch : p[(j - 1) % 2];
+        if (j == J - 1) {
+            d.out[0] = out;
+            d.out_pitch[0] = out_pitch;
+        } else {
+            d.out[0] = buf[j % 2];
+            d.out_pitch[0] = p[j % 2];
+        }
+        d.out[1] = out + wd;
+        d.out[2] = out + hd * out_pitch;
+        d.out[3] = out + hd * out_pitch + wd;
+        d.out_pitch[1] = d.out_pitch[2] = d.out_pitch[3] = out_pitch;
+        plan_level(d, seg_hint);
+        cudaError_t e = launch_level(d, wavelet, false, s, err);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long long out_pitch, int W,
+                          int H, int J, int wavelet, float *scratch, cudaStream_t s, int *err,
+                          int seg_hint)
+{
+    long long p[2];
+    dense_scratch_floats(W, H, J, &p[0], &p[1]);
+    float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
+    for (int j = J; j >= 1; --j) {
+        const int w = ceil_div_pow2(W, j - 1), h = ceil_div_pow2(H, j - 1);
+        const int ws = (w + 1) / 2, hs = (h + 1) / 2;
+        LevelDesc d{};
+        d.w = w;
+        d.h = h;
+        d.in[0] = j == J ? in : buf[(j - 1) % 2];
+        d.in_pitch[0] = j == J ? in_pitch : p[(j - 1) % 2];
+        d.in[1] = in + ws;
+        d.in[2] = in + hs * in_pitch;
+        d.in[3] = in + hs * in_pitch + ws;
+        d.in_pitch[1] = d.in_pitch[2] = d.in_pitch[3] = in_pitch;
+        if (j == 1) {
+            d.out[0] = out;
+            d.out_pitch[0] = out_pitch;
+        } else {
+            d.out[0] = buf[(j - 2) % 2];
+            d.out_pitch[0] = p[(j - 2) % 2];
+        }
+        plan_level(d, seg_hint);
+        cudaError_t e = launch_level(d, wavelet, true, s, err);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// ------------------------------------------------------------ 2D driver
+
+// Validates a caller frame; returns false (and logs) for layouts the
+// library does not take: non-positive sizes with levels to do, negative
+// strides, samples that overlap, an inner frame larger than the outer one.
+static bool frame_ok(int sx, int sy, int ox, int oy, int ix, int iy)
+{
+    if (ox < 0 || oy < 0 || ix < 0 || iy < 0) {
+        log_error("negative image size\n");
+        return false;
+    }
+    if (ix > ox || iy > oy) {
+        log_error("inner image %dx%d larger than the outer frame %dx%d\n", ix, iy, ox, oy);
+        return false;
+    }
+    if (sx <= 0 || sy <= 0) {
+        log_error("strides must be positive (stride_x=%d, stride_y=%d)\n", sx, sy);
+        return false;
+    }
+    const bool rows = (long long)sy >= 4 && (long long)sx >= (long long)ox * sy;
+    const bool cols = (long long)sx >= 4 && (long long)sy >= (long long)oy * sx;
+    if (!(rows || cols) && ox > 1 && oy > 1) {
+        log_error("stride_x=%d / stride_y=%d make samples of a %dx%d frame overlap\n", sx, sy, ox, oy);
+        return false;
+    }
+    return true;
+}
+
+static long long span_bytes(int sx, int sy, int ox, int oy)
+{
+    return (long long)(oy - 1) * sx + (long long)(ox - 1) * sy + 4;
+}
+
+// The whole 2D call.  inverse: j is the requested level count (in); forward:
+// *jp is clamped and written back first.
+static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, int oy, int ix, int iy,
+                  int *jp, int j_in, int decompose_one, int zero_padding)
+{
+    t_last_error = DWT_GPU_OK;
+    if (!frame_ok(sx, sy, ox, oy, ix, iy)) return set_error(DWT_GPU_EINVAL);
+    const int omin = std::min(ox, oy), omax = std::max(ox, oy);
+    const int j_limit = (decompose_one ? omax : omin) > 0 ? ceil_log2_int(decompose_one ? omax : omin) : 0;
+    int J;
+    if (!inverse) {
+        if (*jp < 0 || *jp > j_limit) *jp = j_limit;
+        J = *jp;
+    } else {
+        J = j_limit;
+        if (j_in >= 0 && j_in < J) J = j_in;
+    }
+    if (J == 0 || ox == 0 || oy == 0) return DWT_GPU_OK;
+    if (!ptr) {
+        log_error("null image pointer\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const MemKind kind = classify(ptr);
+    const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
+    const bool dense = (ix == ox && iy == oy);
+    const long long P = align_up(ox, 32);  // compact pitch in floats
+    // a single-row frame may carry any row stride; 2D copies want pitch >= width
+    const long long csx = oy == 1 ? std::max<long long>(sx, 4LL * ox) : sx;
+
+    // 1. stage into IN
+    Buf in(size_t(P) * oy * 4 + 256, s);
+    if (!in.p) return set_error(DWT_GPU_ENOMEM);
+    Buf span;  // host path with a non-4-byte pixel pitch: device copy of the byte span
+    const long long sb = span_bytes(sx, sy, ox, oy);
+    if (!on_device) {
+        if (sy == 4) {
+            CK(cudaMemcpy2DAsync(in.p, P * 4, ptr, csx, size_t(ox) * 4, oy, cudaMemcpyHostToDevice, s));
+        } else {
+            if (!span.alloc(size_t(sb) + 16, s)) return set_error(DWT_GPU_ENOMEM);
+            CK(cudaMemcpyAsync(span.p, ptr, size_t(sb), cudaMemcpyHostToDevice, s));
+            CK(launch_repack(span.p, sx, sy, ox, oy, in.f(), P, s));
+        }
+    } else if (sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0) {
+        CK(cudaMemcpy2DAsync(in.p, P * 4, ptr, csx, size_t(ox) * 4, oy, cudaMemcpyDeviceToDevice, s));
+    } else {
+        CK(launch_repack(ptr, sx, sy, ox, oy, in.f(), P, s));
+    }
+
+    // 2. transform
+    float *out = nullptr;
+    long long out_pitch = 0;
+    Buf outb;
+    const bool direct = on_device && dense && sy == 4 && (csx % 4) == 0 &&
+                        (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
+    if (dense) {
+        if (direct) {
+            out = static_cast<float *>(ptr);
+            out_pitch = csx / 4;
+        } else {
+            if (!outb.alloc(size_t(P) * oy * 4 + 256, s)) return set_error(DWT_GPU_ENOMEM);
+            out = outb.f();
+            out_pitch = P;
+        }
+        long long p0, p1;
+        const size_t sf = dense_scratch_floats(ox, oy, J, &p0, &p1);
+        Buf scratch(sf * 4 + 256, s);
+        if (sf && !scratch.p) return set_error(DWT_GPU_ENOMEM);
+        if (!inverse)
+            CK(dense_forward(in.f(), P, out, out_pitch, ox, oy, J, wavelet, scratch.f(), s, c.d_err, 0));
+        else
+            CK(dense_inverse(in.f(), P, out, out_pitch, ox, oy, J, wavelet, scratch.f(), s, c.d_err, 0));
+    } else {
+        // sparse frame: the reference's per-line sequence, in place on IN
+        const int lmax = std::max(ox, oy);
+        Buf tmp(size_t(lmax) * lmax * 4 + 256, s);
+        if (!tmp.p) return set_error(DWT_GPU_ENOMEM);
+        if (!inverse) {
+            for (int j = 0; j < J; ++j) {
+                CK(sparse_forward_level(in.f(), P, ceil_div_pow2(ox, j), ceil_div_pow2(oy, j),
+                                        ceil_div_pow2(ox, j + 1), ceil_div_pow2(oy, j + 1),
+                                        ceil_div_pow2(ix, j), ceil_div_pow2(iy, j), zero_padding,
+                                        wavelet, tmp.f(), s));
+            }
+        } else {
+            for (int j = J; j >= 1; --j) {
+                CK(sparse_inverse_level(in.f(), P, ceil_div_pow2(ox, j), ceil_div_pow2(oy, j),
+                                        ceil_div_pow2(ox, j - 1), ceil_div_pow2(oy, j - 1),
+                                        ceil_div_pow2(ix, j - 1), ceil_div_pow2(iy, j - 1), zero_padding,
+                                        wavelet, tmp.f(), s));
+            }
+        }
+        out = in.f();
+        out_pitch = P;
+    }
+
+    // 3. write back
+    if (!on_device) {
+        if (sy == 4) {
+            CK(cudaMemcpy2DAsync(ptr, csx, out, out_pitch * 4, size_t(ox) * 4, oy, cudaMemcpyDeviceToHost, s));
+        } else {
+            CK(launch_unpack(out, out_pitch, span.p, sx, sy, ox, oy, s));
+            CK(cudaMemcpyAsync(ptr, span.p, size_t(sb), cudaMemcpyDeviceToHost, s));
+        }
+    } else if (!direct) {
+        CK(launch_unpack(out, out_pitch, ptr, sx, sy, ox, oy, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+// ------------------------------------------------------------ 1D driver
+
+int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l, float *h_out, int N,
+           int stride)
+{
+    t_last_error = DWT_GPU_OK;
+    if (N < 0 || stride == 0) {
+        log_error("invalid 1D arguments (N=%d, stride=%d)\n", N, stride);
+        return set_error(DWT_GPU_EINVAL);
+    }
+    if (N == 0) return DWT_GPU_OK;
+    if (stride < 4) {
+        log_error("stride %d smaller than a sample\n", stride);
+        return set_error(DWT_GPU_EINVAL);
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const int nl = (N + 1) / 2, nh = N / 2;
+    const long long P = align_up(N, 32);
+    Buf in(size_t(P) * 4 + 256, s), out(size_t(P) * 4 + 256, s);
+    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
+
+    // stage the input samples into IN (forward: N samples; inverse: L then H)
+    auto gather = [&](const float *src, float *dst, int n) -> cudaError_t {
+        if (n == 0) return cudaSuccess;
+        const MemKind k = classify(src);
+        if (k == MemKind::Device || k == MemKind::Managed)
+            return launch_gather_signals(src, n, stride, 1, 1, 0, 0, dst, P, s);
+        return cudaMemcpy2DAsync(dst, 4, src, stride, 4, n, cudaMemcpyHostToDevice, s);
+    };
+    auto scatter = [&](const float *src, float *dst, int n) -> cudaError_t {
+        if (n == 0) return cudaSuccess;
+        const MemKind k = classify(dst);
+        if (k == MemKind::Device || k == MemKind::Managed)
+            return launch_scatter_signals(src, P, n, dst, stride, 1, 1, 0, 0, s);
+        return cudaMemcpy2DAsync(dst, stride, src, 4, 4, n, cudaMemcpyDeviceToHost, s);
+    };
+
+    LevelDesc d{};
+    d.w = N;
+    d.h = 1;
+    d.rows_only = 1;
+    if (!inverse) {
+        CK(gather(a, in.f(), N));
+        d.in[0] = in.f();
+        d.in_pitch[0] = P;
+        d.out[0] = out.f();
+        d.out[1] = out.f() + nl;
+        d.out_pitch[0] = d.out_pitch[1] = P;
+    } else {
+        // L at IN[0, nl), H at IN[nl4, ...) with nl4 16-byte aligned
+        const int nl4 = int(align_up(nl, 4));
+        CK(gather(a, in.f(), nl));
+        CK(gather(b, in.f() + nl4, nh));
+        d.in[0] = in.f();
+        d.in[1] = in.f() + nl4;
+        d.in_pitch[0] = d.in_pitch[1] = P;
+        d.out[0] = out.f();
+        d.out_pitch[0] = P;
+    }
+    plan_level(d, 0);
+    CK(launch_level(d, wavelet, inverse, s, c.d_err));
+    if (!inverse) {
+        CK(scatter(out.f(), c_l, nl));
+        CK(scatter(out.f() + nl, h_out, nh));
+    } else {
+        CK(scatter(out.f(), c_l, N));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+// Batched strided 1D, in place: gather every signal into a row of IN,
+// transform all rows in one launch, scatter back.
+int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long long count, int group,
+                 long long group_stride, int lane_stride)
+{
+    t_last_error = DWT_GPU_OK;
+    if (N < 0 || stride < 4 || count < 0 || group <= 0 || !base) {
+        log_error("invalid batched 1D arguments\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+    if (N == 0 || count == 0) return DWT_GPU_OK;
+    if (count > 0x7fffffffLL) return set_error(DWT_GPU_EINVAL);
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const MemKind kind = classify(base);
+    const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
+    const int nl = (N + 1) / 2;
+    const long long P = align_up(N + 4, 32);
+    const int nl4 = int(align_up(nl, 4));
+    Buf in(size_t(P) * count * 4 + 256, s), out(size_t(P) * count * 4 + 256, s);
+    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
+
+    // the bank's byte span (for host memory)
+    const long long last = (count - 1) / group * group_stride + (count - 1) % group * (long long)lane_stride;
+    const long long sb = last + (long long)(N - 1) * stride + 4;
+    Buf span;
+    const void *src = base;
+    if (!on_device) {
+        if (!span.alloc(size_t(sb) + 16, s)) return set_error(DWT_GPU_ENOMEM);
+        CK(cudaMemcpyAsync(span.p, base, size_t(sb), cudaMemcpyHostToDevice, s));
+        src = span.p;
+    }
+    LevelDesc d{};
+    d.w = N;
+    d.h = int(count);
+    d.rows_only = 1;
+    if (!inverse) {
+        CK(launch_gather_signals(src, N, stride, count, group, group_stride, lane_stride, in.f(), P, s));
+        d.in[0] = in.f();
+        d.in_pitch[0] = P;
+        d.out[0] = out.f();
+        d.out[1] = out.f() + nl;
+        d.out_pitch[0] = d.out_pitch[1] = P;
+    } else {
+        // L samples to columns [0, nl), H samples to [nl4, nl4 + N/2) of each row
+        CK(launch_gather_signals(src, nl, stride, count, group, group_stride, lane_stride, in.f(), P, s));
+        CK(launch_gather_signals(static_cast<const char *>(src) + (long long)nl * stride, N / 2, stride,
+                                 count, group, group_stride, lane_stride, in.f() + nl4, P, s));
+        d.in[0] = in.f();
+        d.in[1] = in.f() + nl4;
+        d.in_pitch[0] = d.in_pitch[1] = P;
+        d.out[0] = out.f();
+        d.out_pitch[0] = P;
+    }
+    plan_level(d, 0);
+    CK(launch_level(d, wavelet, inverse, s, c.d_err));
+    void *dst = on_device ? base : span.p;
+    CK(launch_scatter_signals(out.f(), P, N, dst, stride, count, group, group_stride, lane_stride, s));
+    if (!on_device) CK(cudaMemcpyAsync(base, span.p, size_t(sb), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_bytes, float *dst,
+               long long dst_pitch_bytes, int w, int h, int j_levels, int decompose_one, cudaStream_t s)
+{
+    t_last_error = DWT_GPU_OK;
+    if (w <= 0 || h <= 0 || !src || !dst || (src_pitch_bytes % 16) != 0 ||
+        (reinterpret_cast<uintptr_t>(src) & 15) != 0 || (dst_pitch_bytes % 4) != 0 ||
+        src_pitch_bytes < 4LL * w || dst_pitch_bytes < 4LL * w) {
+        log_error("invalid device 2D arguments\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+    const int lim = ceil_log2_int(decompose_one ? std::max(w, h) : std::min(w, h));
+    const int J = (j_levels < 0 || j_levels > lim) ? lim : j_levels;
+    if (J == 0) {
+        if (src != dst)
+            CK(cudaMemcpy2DAsync(dst, dst_pitch_bytes, src, src_pitch_bytes, size_t(w) * 4, h,
+                                 cudaMemcpyDeviceToDevice, s));
+        return 0;
+    }
+    Context &c = ctx();
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(w, h, J, &p0, &p1);
+    void *scratch = sf ? c.pool.alloc(sf * 4 + 256, s) : nullptr;
+    if (sf && !scratch) return set_error(DWT_GPU_ENOMEM);
+    cudaError_t e = inverse ? dense_inverse(src, src_pitch_bytes / 4, dst, dst_pitch_bytes / 4, w, h, J,
+                                            wavelet, static_cast<float *>(scratch), s, c.d_err, 0)
+                            : dense_forward(src, src_pitch_bytes / 4, dst, dst_pitch_bytes / 4, w, h, J,
+                                            wavelet, static_cast<float *>(scratch), s, c.d_err, 0);
+    if (scratch) c.pool.release(scratch, s);
+    if (e != cudaSuccess) {
+        log_error("CUDA error %s\n", cudaGetErrorString(e));
+        return set_error(DWT_GPU_ECUDA);
+    }
+    return J;
+}
+
+}  // namespace dwt
+
+using namespace dwt;
+
+// ====================================================================== C ABI
+
+static void die_if(int rc)
+{
+    if (rc != DWT_GPU_OK) {
+        log_error("libdwt_gb300: %s\n", dwt_gpu_error_string(rc));
+        abort();  // the reference's fatal-error convention (src/libdwt.c:7512-7530)
+    }
+}
+
+extern "C" {
+
+int dwt_gpu_get_last_error(void) { return t_last_error; }
+
+const char *dwt_gpu_error_string(int code)
+{
+    switch (code) {
+    case DWT_GPU_OK: return "success";
+    case DWT_GPU_EINVAL: return "invalid argument";
+    case DWT_GPU_ECUDA: return "CUDA error";
+    case DWT_GPU_ENOMEM: return "out of device memory";
+    case DWT_GPU_EDEVICE: return "device-side wait gave up";
+    case DWT_GPU_EBUSY: return "admission refused";
+    case DWT_GPU_ENOTFOUND: return "unknown request";
+    default: return "unknown error";
+    }
+}
+
+int dwt_gpu_2f_s(int wavelet, void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy,
+                 int *j_max_ptr, int decompose_one, int zero_padding)
+{
+    if (!j_max_ptr || (wavelet != CDF97 && wavelet != CDF53)) return set_error(DWT_GPU_EINVAL);
+    return run_2d(wavelet, false, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, 0, decompose_one,
+                  zero_padding);
+}
+
+int dwt_gpu_2i_s(int wavelet, void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy,
+                 int j_max, int decompose_one, int zero_padding)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_2d(wavelet, true, ptr, stride_x, stride_y, ox, oy, ix, iy, nullptr, j_max, decompose_one,
+                  zero_padding);
+}
+
+int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float *c_or_l, float *h_or_null,
+                int N, int stride)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_1d(wavelet, inverse != 0, a, b, c_or_l, h_or_null, N, stride);
+}
+
+int dwt_gpu_2_dev(int wavelet, int inverse, const float *src, long long src_pitch_bytes, float *dst,
+                  long long dst_pitch_bytes, int w, int h, int j_levels, int decompose_one, void *stream)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_2d_dev(wavelet, inverse != 0, src, src_pitch_bytes, dst, dst_pitch_bytes, w, h, j_levels,
+                      decompose_one, static_cast<cudaStream_t>(stream));
+}
+
+int dwt_gpu_1_batch_s(int wavelet, int inverse, void *base, int N, int stride, long long count, int group,
+                      long long group_stride, int lane_stride)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_1d_batch(wavelet, inverse != 0, base, N, stride, count, group, group_stride, lane_stride);
+}
+
+void dwt_cdf97_2f_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2f_s(CDF97, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, decompose_one, zero_padding));
+}
+
+void dwt_cdf53_2f_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2f_s(CDF53, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, decompose_one, zero_padding));
+}
+
+void dwt_cdf97_2i_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int j_max,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2i_s(CDF97, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max, decompose_one, zero_padding));
+}
+
+void dwt_cdf53_2i_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int j_max,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2i_s(CDF53, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max, decompose_one, zero_padding));
+}
+
+void dwt_cdf97_f_ex_stride_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d(CDF97, false, src, nullptr, dst_l, dst_h, N, stride));
+}
+
+void dwt_cdf97_i_ex_stride_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d(CDF97, true, src_l, src_h, dst, nullptr, N, stride));
+}
+
+void dwt_cdf53_f_ex_stride_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d(CDF53, false, src, nullptr, dst_l, dst_h, N, stride));
+}
+
+void dwt_cdf53_i_ex_stride_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d(CDF53, true, src_l, src_h, dst, nullptr, N, stride));
+}
+
+void dwt_cdf97_f_ex_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N)
+{
+    dwt_cdf97_f_ex_stride_s(src, dst_l, dst_h, tmp, N, sizeof(float));
+}
+
+void dwt_cdf53_f_ex_s(const float *src, float *dst_l, float *dst_h, float *tmp, int N)
+{
+    dwt_cdf53_f_ex_stride_s(src, dst_l, dst_h, tmp, N, sizeof(float));
+}
+
+void dwt_cdf97_i_ex_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N)
+{
+    dwt_cdf97_i_ex_stride_s(src_l, src_h, dst, tmp, N, sizeof(float));
+}
+
+void dwt_cdf53_i_ex_s(const float *src_l, const float *src_h, float *dst, float *tmp, int N)
+{
+    dwt_cdf53_i_ex_stride_s(src_l, src_h, dst, tmp, N, sizeof(float));
+}
+
+void dwt_cdf97_f_s(const float *src, float *dst, float *tmp, int N)
+{
+    dwt_cdf97_f_ex_s(src, dst, dst + (N + 1) / 2, tmp, N);
+}
+
+void dwt_cdf53_f_s(const float *src, float *dst, float *tmp, int N)
+{
+    dwt_cdf53_f_ex_s(src, dst, dst + (N + 1) / 2, tmp, N);
+}
+
+void dwt_cdf97_i_s(const float *src, float *dst, float *tmp, int N)
+{
+    dwt_cdf97_i_ex_s(src, src + (N + 1) / 2, dst, tmp, N);
+}
+
+void dwt_cdf53_i_s(const float *src, float *dst, float *tmp, int N)
+{
+    dwt_cdf53_i_ex_s(src, src + (N + 1) / 2, dst, tmp, N);
+}
+
+void dwt_util_init(void) { (void)ctx(); }
+
+void dwt_util_finish(void) { ctx_finish(); }
+
+void dwt_util_set_accel(int accel_type) { g_accel.store(accel_type); }
+
+int dwt_util_ceil_log2(int x) { return ceil_log2_int(x); }
+
+int dwt_util_pow2_ceil_log2(int x) { return 1 << ceil_log2_int(x); }
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// Shared device helpers of the GB300 lifting kernels: lifting parameters,
+// symmetric-extension index mapping, exact (non-contracted) float arithmetic,
+// and thin inline-PTX wrappers for mbarriers and the TMA bulk-copy engine.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dwt {
+
+// Lifting parameters of one wavelet, in the order the steps are applied.
+//
+// Forward: steps c[0..n) alternate odd, even, odd, even samples; then even
+// samples are multiplied by zeta_e and odd ones by zeta_o.
+// Inverse: even samples are multiplied by zeta_o and odd ones by zeta_e; then
+// steps c[0..n) alternate even, odd, even, odd samples.
+// A signal of length 1 is only scaled: by n1 (n1_fwd / n1_inv).
+//
+// CDF 9/7 (src/libdwt.c:541-547, 5543, 5811):
+//   forward (-p1, u1, -p2, u2), zeta_e = s1, zeta_o = 1/s1 rounded as a float
+//   division; inverse (-u2, p2, -u1, p1); n1_inv = the constant s2.
+// CDF 5/3 (src/libdwt.c:566-569, 5571-5592, 5838-5864):
+//   forward (-p1, u1), zeta_e = s1, zeta_o = s2; inverse (-u1, p1).
+struct Wavelet {
+    float c[4];
+    float zeta_e, zeta_o;
+    float n1_fwd, n1_inv;
+    int nsteps;
+};
+
+enum WaveletId { CDF97 = 0, CDF53 = 1 };
+
+// Host-side construction (float arithmetic on the host matches the device).
+Wavelet make_wavelet(int id, bool inverse);
+
+// Exact IEEE single operations that the compiler may not fuse into an FMA.
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+// x + c*(l + r), three separately rounded operations.
+__device__ __forceinline__ float lift(float x, float c, float l, float r)
+{
+    return fadd(x, fmul(c, fadd(l, r)));
+}
+
+// Whole-sample symmetric extension of index r into [0, n), n >= 2: the
+// periodic reflection with period 2(n-1).  Keeps the parity of r.
+__host__ __device__ __forceinline__ int mirror(int r, int n)
+{
+    if (n <= 1) return 0;
+    const int p = 2 * (n - 1);
+    int m = r % p;
+    if (m < 0) m += p;
+    return (m >= n) ? p - m : m;
+}
+
+__host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+__host__ __device__ __forceinline__ int ceil_div_pow2(int i, int j) { return (i + (1 << j) - 1) >> j; }
+
+// ---------------------------------------------------------------- PTX wrappers
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.  try_wait itself suspends for a
+// hardware-chosen interval, so the iteration cap is seconds of wall time.
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// TMA bulk copy global -> shared, completion signalled on `bar` as bytes.
+// dst and src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Error codes raised by device code into the error word.
+enum DeviceError : int {
+    kErrNone = 0,
+    kErrWaitTimeout = 1,   // an mbarrier wait gave up
+    kErrQueueTimeout = 2,  // a work-queue dependency wait gave up
+};
+
+}  // namespace dwt

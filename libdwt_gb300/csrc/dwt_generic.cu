@@ -1,0 +1,247 @@
+// Layout and frame kernels around the fused level kernel:
+//   * repack / unpack between the caller's byte-strided layout (any byte
+//     strides, floats possibly not 4-byte aligned) and a compact row-major
+//     float frame with a 16-byte aligned pitch;
+//   * the per-line path for sparse frames (outer size > inner size), which
+//     must keep the reference's exact in-place semantics: a line pass writes
+//     L to [0, ceil(n/2)) and H from the outer midpoint, leaving the samples
+//     in between untouched (src/libdwt.c:6354-6375), then optional zero
+//     padding (src/libdwt.c:6377-6397, 6729-6745).
+#include "dwt_generic.cuh"
+
+namespace dwt {
+
+namespace {
+
+__device__ __forceinline__ float load_any(const unsigned char *p)
+{
+    if ((reinterpret_cast<uintptr_t>(p) & 3) == 0) return *reinterpret_cast<const float *>(p);
+    uint32_t u = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
+    return __uint_as_float(u);
+}
+
+__device__ __forceinline__ void store_any(unsigned char *p, float v)
+{
+    if ((reinterpret_cast<uintptr_t>(p) & 3) == 0) {
+        *reinterpret_cast<float *>(p) = v;
+        return;
+    }
+    const uint32_t u = __float_as_uint(v);
+    p[0] = u & 0xff;
+    p[1] = (u >> 8) & 0xff;
+    p[2] = (u >> 16) & 0xff;
+    p[3] = (u >> 24) & 0xff;
+}
+
+__global__ void repack_kernel(const unsigned char *src, long long sx, long long sy, int ox, int oy,
+                              float *dst, long long dpitch)
+{
+    const long long n = (long long)ox * oy;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int y = int(k / ox), x = int(k % ox);
+        dst[y * dpitch + x] = load_any(src + y * sx + x * sy);
+    }
+}
+
+__global__ void unpack_kernel(const float *src, long long spitch, unsigned char *dst, long long sx,
+                              long long sy, int ox, int oy)
+{
+    const long long n = (long long)ox * oy;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int y = int(k / ox), x = int(k % ox);
+        store_any(dst + y * sx + x * sy, src[y * spitch + x]);
+    }
+}
+
+// Strided signal gather/scatter: signal s, sample i lives at byte offset
+// (s / group) * group_stride + (s % group) * lane_stride + i * stride.
+__global__ void gather_signals_kernel(const unsigned char *base, int N, long long stride, long long count,
+                                      int group, long long group_stride, long long lane_stride,
+                                      float *dst, long long dpitch)
+{
+    const long long n = (long long)N * count;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long s = k / N;
+        const int i = int(k % N);
+        const unsigned char *p = base + (s / group) * group_stride + (s % group) * lane_stride + i * stride;
+        dst[s * dpitch + i] = load_any(p);
+    }
+}
+
+__global__ void scatter_signals_kernel(const float *src, long long spitch, int N, unsigned char *base,
+                                       long long stride, long long count, int group,
+                                       long long group_stride, long long lane_stride)
+{
+    const long long n = (long long)N * count;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long s = k / N;
+        const int i = int(k % N);
+        unsigned char *p = base + (s / group) * group_stride + (s % group) * lane_stride + i * stride;
+        store_any(p, src[s * spitch + i]);
+    }
+}
+
+// One lifting step on the samples of `parity` of a line held in tmp with
+// element stride ts (lines interleaved so threads of a warp coalesce).
+__device__ __forceinline__ void line_step(float *x, long long ts, int N, int parity, float c)
+{
+    for (int i = parity; i < N; i += 2) {
+        const float l = (i > 0) ? x[(i - 1) * ts] : x[(i + 1) * ts];
+        const float r = (i + 1 < N) ? x[(i + 1) * ts] : x[(i - 1) * ts];
+        x[i * ts] = lift(x[i * ts], c, l, r);
+    }
+}
+
+__device__ __forceinline__ void line_scale(float *x, long long ts, int N, float even, float odd)
+{
+    for (int i = 0; i < N; i += 2) x[i * ts] = fmul(x[i * ts], even);
+    for (int i = 1; i < N; i += 2) x[i * ts] = fmul(x[i * ts], odd);
+}
+
+// Forward per-line transform in place on a compact frame: line k starts at
+// base + k*ls, samples es apart.  Reads N samples, writes L to [0, ceil(N/2))
+// and H to [hoff, hoff + floor(N/2)).  One thread per line.
+__global__ void lines_forward_kernel(float *base, long long ls, long long es, int nlines, int N,
+                                     int hoff, float *tmp, const Wavelet W)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines || N <= 0) return;
+    float *line = base + k * ls;
+    if (N == 1) {
+        line[0] = fmul(line[0], W.n1_fwd);
+        return;
+    }
+    float *x = tmp + k;
+    const long long ts = nlines;
+    for (int i = 0; i < N; ++i) x[i * ts] = line[i * es];
+    for (int s = 0; s < W.nsteps; ++s) line_step(x, ts, N, (s & 1) ? 0 : 1, W.c[s]);
+    line_scale(x, ts, N, W.zeta_e, W.zeta_o);
+    for (int i = 0; 2 * i < N; ++i) line[i * es] = x[(2 * i) * ts];
+    for (int i = 0; 2 * i + 1 < N; ++i) line[(hoff + i) * es] = x[(2 * i + 1) * ts];
+}
+
+// Inverse per-line transform: L from [0, ceil(N/2)), H from [hoff, ...),
+// result to [0, N).
+__global__ void lines_inverse_kernel(float *base, long long ls, long long es, int nlines, int N,
+                                     int hoff, float *tmp, const Wavelet W)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines || N <= 0) return;
+    float *line = base + k * ls;
+    if (N == 1) {
+        line[0] = fmul(line[0], W.n1_inv);
+        return;
+    }
+    float *x = tmp + k;
+    const long long ts = nlines;
+    for (int i = 0; 2 * i < N; ++i) x[(2 * i) * ts] = line[i * es];
+    for (int i = 0; 2 * i + 1 < N; ++i) x[(2 * i + 1) * ts] = line[(hoff + i) * es];
+    line_scale(x, ts, N, W.zeta_o, W.zeta_e);
+    for (int s = 0; s < W.nsteps; ++s) line_step(x, ts, N, (s & 1) ? 1 : 0, W.c[s]);
+    for (int i = 0; i < N; ++i) line[i * es] = x[i * ts];
+}
+
+// Zero padding of a forward level (dwt_zero_padding_f_stride_s): per line,
+// zero L samples [ceil(N/2), nL) and H samples [floor(N/2), nH) from hoff.
+__global__ void zero_forward_kernel(float *base, long long ls, long long es, int nlines, int N, int nL,
+                                    int nH, int hoff)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines || (nL == 0 && nH == 0)) return;
+    float *line = base + k * ls;
+    for (int i = (N + 1) / 2; i < nL; ++i) line[i * es] = 0.0f;
+    for (int i = N / 2; i < nH; ++i) line[(hoff + i) * es] = 0.0f;
+}
+
+// Zero padding of an inverse level (dwt_zero_padding_i_stride_s).
+__global__ void zero_inverse_kernel(float *base, long long ls, long long es, int nlines, int N, int n_dst)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines) return;
+    float *line = base + k * ls;
+    for (int i = N; i < n_dst; ++i) line[i * es] = 0.0f;
+}
+
+int grid_for(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    if (g > 152LL * 32) g = 152LL * 32;
+    if (g < 1) g = 1;
+    return int(g);
+}
+
+}  // namespace
+
+cudaError_t launch_repack(const void *src, long long sx, long long sy, int ox, int oy, float *dst,
+                          long long dpitch, cudaStream_t s)
+{
+    if ((long long)ox * oy == 0) return cudaSuccess;
+    repack_kernel<<<grid_for((long long)ox * oy, 256), 256, 0, s>>>(
+        static_cast<const unsigned char *>(src), sx, sy, ox, oy, dst, dpitch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long long sx, long long sy,
+                          int ox, int oy, cudaStream_t s)
+{
+    if ((long long)ox * oy == 0) return cudaSuccess;
+    unpack_kernel<<<grid_for((long long)ox * oy, 256), 256, 0, s>>>(
+        src, spitch, static_cast<unsigned char *>(dst), sx, sy, ox, oy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_signals(const void *base, int N, long long stride, long long count, int group,
+                                  long long group_stride, long long lane_stride, float *dst,
+                                  long long dpitch, cudaStream_t s)
+{
+    if ((long long)N * count == 0) return cudaSuccess;
+    gather_signals_kernel<<<grid_for((long long)N * count, 256), 256, 0, s>>>(
+        static_cast<const unsigned char *>(base), N, stride, count, group, group_stride, lane_stride, dst,
+        dpitch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, void *base, long long stride,
+                                   long long count, int group, long long group_stride,
+                                   long long lane_stride, cudaStream_t s)
+{
+    if ((long long)N * count == 0) return cudaSuccess;
+    scatter_signals_kernel<<<grid_for((long long)N * count, 256), 256, 0, s>>>(
+        src, spitch, N, static_cast<unsigned char *>(base), stride, count, group, group_stride,
+        lane_stride);
+    return cudaGetLastError();
+}
+
+// Sparse-frame level on a compact frame `f` (pitch in floats), in place, the
+// reference driver's exact sequence.  tmp holds max(lines) * max(len) floats.
+cudaError_t sparse_forward_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int isx,
+                                 int isy, int zero_padding, int wavelet, float *tmp, cudaStream_t s)
+{
+    const Wavelet W = make_wavelet(wavelet, false);
+    lines_forward_kernel<<<ceil_div(osy, 128), 128, 0, s>>>(f, pitch, 1, osy, isx, odx, tmp, W);
+    lines_forward_kernel<<<ceil_div(osx, 128), 128, 0, s>>>(f, 1, pitch, osx, isy, ody, tmp, W);
+    if (zero_padding) {
+        zero_forward_kernel<<<ceil_div(osy, 128), 128, 0, s>>>(f, pitch, 1, osy, isx, odx, osx - odx, odx);
+        zero_forward_kernel<<<ceil_div(osx, 128), 128, 0, s>>>(f, 1, pitch, osx, isy, ody, osy - ody, ody);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t sparse_inverse_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int idx,
+                                 int idy, int zero_padding, int wavelet, float *tmp, cudaStream_t s)
+{
+    const Wavelet W = make_wavelet(wavelet, true);
+    lines_inverse_kernel<<<ceil_div(ody, 128), 128, 0, s>>>(f, pitch, 1, ody, idx, osx, tmp, W);
+    lines_inverse_kernel<<<ceil_div(odx, 128), 128, 0, s>>>(f, 1, pitch, odx, idy, osy, tmp, W);
+    if (zero_padding) {
+        zero_inverse_kernel<<<ceil_div(ody, 128), 128, 0, s>>>(f, pitch, 1, ody, idx, odx);
+        zero_inverse_kernel<<<ceil_div(odx, 128), 128, 0, s>>>(f, 1, pitch, odx, idy, ody);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace dwt

@@ -1,0 +1,29 @@
+// Layout repacking and the per-line sparse-frame path (see dwt_generic.cu).
+#pragma once
+
+#include "dwt_common.cuh"
+
+namespace dwt {
+
+// caller layout (byte strides, any alignment) -> compact float frame
+cudaError_t launch_repack(const void *src, long long sx, long long sy, int ox, int oy, float *dst,
+                          long long dpitch, cudaStream_t s);
+// compact float frame -> caller layout; touches only the frame's samples
+cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long long sx, long long sy,
+                          int ox, int oy, cudaStream_t s);
+
+// strided signal bank <-> compact rows (one signal per row)
+cudaError_t launch_gather_signals(const void *base, int N, long long stride, long long count, int group,
+                                  long long group_stride, long long lane_stride, float *dst,
+                                  long long dpitch, cudaStream_t s);
+cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, void *base, long long stride,
+                                   long long count, int group, long long group_stride,
+                                   long long lane_stride, cudaStream_t s);
+
+// One level of a sparse frame (outer > inner), in place on a compact frame.
+cudaError_t sparse_forward_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int isx,
+                                 int isy, int zero_padding, int wavelet, float *tmp, cudaStream_t s);
+cudaError_t sparse_inverse_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int idx,
+                                 int idy, int zero_padding, int wavelet, float *tmp, cudaStream_t s);
+
+}  // namespace dwt

@@ -1,0 +1,48 @@
+// One decomposition level of the 2D lifting transform, fused rows + columns,
+// out of place: the forward reads one interleaved image and writes the four
+// bands LL, HL, LH, HH; the inverse reads the four bands and writes the
+// interleaved image.  Declarations shared by the host launchers.
+#pragma once
+
+#include "dwt_common.cuh"
+
+namespace dwt {
+
+// Work decomposition: a warp holds kStripIn interleaved columns of a row
+// (4 per lane) and produces the kStripOut middle ones; lanes 0 and 31 are the
+// lifting halo.  Rows are walked as (even, odd) pairs in segments of
+// seg_pairs output pairs, each segment warmed up by the lifting latency.
+constexpr int kLanes = 32;
+constexpr int kStripIn = 128;
+constexpr int kStripOut = 120;
+constexpr int kSlotF = 136;        // floats per forward row slot
+constexpr int kSlotI = 68;         // floats per inverse band-row slot
+constexpr int kStageFloats = 272;  // one pipeline stage = 2 rows or 4 band rows
+constexpr int kStages = 8;         // pipeline depth per warp
+constexpr int kWarpsPerCta = 4;
+constexpr int kSmemBytes = kWarpsPerCta * (kStages * kStageFloats * 4 + kStages * 8);
+
+// One level of one image.  Forward: in[0] is the interleaved w x h source,
+// out[0..3] receive LL, HL, LH, HH.  Inverse: in[0..3] are LL, HL, LH, HH,
+// out[0] receives the interleaved w x h image.  Pitches are in floats.
+// Sources must have 16-byte aligned rows (pitch % 4 == 0, 16-byte aligned
+// base for out-of-band reads); destinations need 4-byte alignment only.
+// rows_only: transform rows only (1D signals stored as rows), no vertical step.
+struct LevelDesc {
+    int w, h;
+    int n_strips, seg_pairs, n_segs;
+    int rows_only;
+    const float *in[4];
+    long long in_pitch[4];
+    float *out[4];
+    long long out_pitch[4];
+};
+
+// Fills n_strips / seg_pairs / n_segs for a level of size w x h.
+void plan_level(LevelDesc &d, int seg_pairs_hint);
+
+// Launch one level on `stream`.  err: device error word (may be null).
+cudaError_t launch_level(const LevelDesc &d, int wavelet, bool inverse, cudaStream_t stream,
+                         int *err);
+
+}  // namespace dwt
