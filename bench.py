@@ -1,0 +1,439 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 lifting hot path.
+
+Workload (one GPU): a 16384 x 16384 float32 image (1 GiB, seeded smooth field
+plus noise, integers in [0, 255]) under CDF 9/7, forward then inverse to the
+full depth of 14 levels.  One step = that forward + inverse pair, so one step
+processes 2 * 16384^2 pixels.
+
+Printed JSON line (rank 0):
+  value      Mpx/s of the step with the image resident in HBM (device API,
+             out of place, CUDA events on the launching stream);
+  e2e        the same metric through the drop-in C ABI (dwt_cdf97_2f_s /
+             dwt_cdf97_2i_s) on a pinned host image: every step copies the
+             image to the device and the coefficients / reconstruction back;
+  roofline   the dominant kernel (level 0 of the forward transform) timed
+             alone: algorithmic bytes (read + write, 8 B per pixel) over its
+             average duration, against the measured HBM copy peak;
+  cpu_baseline  the CPU restatement of the reference (OpenMP, all host
+             cores) on the same image.
+The inputs (1 GiB) are larger than L2 (129 MB), so no flush between steps.
+
+--impl reference times the reference algorithm on the host cores (the
+oracle's C restatement, since the reference library itself is compiled only
+where its source is present) and prints the same line with impl=reference.
+
+Multi-GPU: the path does not shard (one image per GPU); N GPUs run N
+independent replicas and `value` is the pixels of all ranks over the slowest
+rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 16384
+J = 14
+WORKLOAD = "cdf97 2D forward+inverse, 16384x16384 float32, j_max=14"
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks + throttle reasons every 100 ms in the background."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        win = [s for (t, s) in self.samples if t0 - 0.15 <= t <= t1 + 0.15]
+        if not win:
+            win = [s for (_, s) in self.samples]
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        mhz = [float(s[1]) for s in win if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in win if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in win for i in range(4) if len(s) > 5 + i and s[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(mhz)) if mhz else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(win)}
+
+
+def cpu_baseline(img: np.ndarray, threads: int, min_s: float = 10.0, max_s: float = 30.0):
+    """Time the oracle (C restatement of the reference, OpenMP on `threads`
+    cores) on the workload: forward + inverse CDF 9/7 of the image, repeated
+    until at least `min_s` seconds of CPU work; a band of full-width rows is
+    used instead of the whole image only if one pair would exceed `max_s`."""
+    from oracle import oracle as O
+    probe = np.ascontiguousarray(img[:512])
+    t = time.perf_counter()
+    f, j = O.transform2_dense(probe, "cdf97", "f", -1, 0, "s", threads)
+    O.transform2_dense(f, "cdf97", "i", j, 0, "s", threads)
+    per_px = (time.perf_counter() - t) / (2 * probe.size)
+    rows = img.shape[0]
+    if per_px * 2 * img.size > max_s:
+        rows = max(512, int(max_s / (per_px * 2 * img.shape[1])))
+    sample = np.ascontiguousarray(img[:rows])
+    pairs, t0 = 0, time.perf_counter()
+    while True:
+        f, j = O.transform2_dense(sample, "cdf97", "f", -1, 0, "s", threads)
+        O.transform2_dense(f, "cdf97", "i", j, 0, "s", threads)
+        pairs += 1
+        if time.perf_counter() - t0 >= min_s:
+            break
+    dt = time.perf_counter() - t0
+    mpx = pairs * 2 * sample.size / dt / 1e6
+    return mpx, (f"{sample.shape[1]}x{sample.shape[0]} cdf97 forward+inverse full depth, "
+                 f"{pairs} pairs in {dt:.1f} s")
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND") != "gloo" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    threads = O.max_threads()
+    img = synth_image()
+    # one step = forward + inverse on a band of full-width rows, sized so the
+    # whole run stays within about two minutes
+    from oracle import oracle as O2
+    strip = np.ascontiguousarray(img[:256])
+    t = time.perf_counter()
+    f, j = O2.transform2_dense(strip, "cdf97", "f", -1, 0, "s", threads)
+    O2.transform2_dense(f, "cdf97", "i", j, 0, "s", threads)
+    per_px = (time.perf_counter() - t) / (2 * strip.size)
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    rows = int(min(H, max(256, budget / (per_px * 2 * W))))
+    sample = np.ascontiguousarray(img[:rows])
+    for _ in range(args.warmup):
+        f, j = O2.transform2_dense(sample, "cdf97", "f", -1, 0, "s", threads)
+        O2.transform2_dense(f, "cdf97", "i", j, 0, "s", threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        f, j = O2.transform2_dense(sample, "cdf97", "f", -1, 0, "s", threads)
+        O2.transform2_dense(f, "cdf97", "i", j, 0, "s", threads)
+    dt = time.perf_counter() - t
+    mpx = args.steps * 2 * sample.size / dt / 1e6
+    desc = f"{W}x{rows} rows of the workload image, cdf97 forward+inverse full depth per step"
+    line = {"impl": "reference", "metric": "2D DWT throughput (CDF 9/7 forward+inverse, full depth)",
+            "value": round(mpx, 3), "unit": "Mpx/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blob field + noise, integers 0..255)",
+            "config": {"workload": WORKLOAD, "sample": desc, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": round(mpx, 3), "unit": "Mpx/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": round(mpx, 3), "unit": "Mpx/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+_IMG = None
+
+
+def synth_image():
+    global _IMG
+    if _IMG is None:
+        from libdwt_gb300 import synth
+        _IMG = synth.image(W, H, seed=0)
+    return _IMG
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--level-reps", type=int, default=50)
+    ap.add_argument("--image", type=int, default=16384,
+                    help="image side (a smaller case for profiler captures)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    global W, H, J, WORKLOAD
+    if args.image != 16384:
+        W = H = args.image
+        J = int(np.ceil(np.log2(W)))
+        WORKLOAD = f"cdf97 2D forward+inverse, {W}x{H} float32, j_max={J}"
+
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import libdwt_gb300 as D
+
+    torch.cuda.set_device(local)
+    D.lib()
+    img = synth_image()
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    src = torch.from_numpy(img).cuda()
+    coef = torch.empty_like(src)
+    rec = torch.empty_like(src)
+
+    def step():
+        D.transform2_dev(src, coef, "cdf97", False, J, 0, sptr)
+        D.transform2_dev(coef, rec, "cdf97", True, J, 0, sptr)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tw1 = time.time()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    ms = allmax(ws, ms)
+    if D.lib().dwt_gpu_sync_check() != 0:
+        raise SystemExit("device error during the timed region")
+    px_step = 2 * W * H
+    value = ws * args.steps * px_step / (ms / 1e3) / 1e6
+
+    # parity spot check of the benchmarked output (outside the timed region):
+    # the reconstruction is within the reference's round-trip tolerance
+    err_rt = float((rec - src).abs().max().item())
+
+    # dominant kernel alone: forward level 0 (16384^2 -> four bands)
+    bands = torch.empty_like(src)
+    ll = torch.empty((H // 2, W // 2), dtype=torch.float32, device="cuda")
+    hw, hh = W // 2, H // 2
+    outs = [ll.data_ptr(), bands.data_ptr() + hw * 4, bands.data_ptr() + hh * W * 4,
+            bands.data_ptr() + (hh * W + hw) * 4]
+    pitches = [hw * 4, W * 4, W * 4, W * 4]
+    reps = max(1, args.level_reps)
+    for _ in range(3):
+        D.level_dev("cdf97", False, W, H, [src.data_ptr()], [W * 4], outs, pitches, sptr)
+    torch.cuda.synchronize()
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    tk0 = time.time()
+    k0.record(stream)
+    for _ in range(reps):
+        D.level_dev("cdf97", False, W, H, [src.data_ptr()], [W * 4], outs, pitches, sptr)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    tk1 = time.time()
+    kms = k0.elapsed_time(k1) / reps
+    alg_bytes = 8 * W * H
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    peak, peak_kind = hbm_peak()
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "level0_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    # e2e through the drop-in C ABI on a pinned host image
+    if args.skip_e2e:
+        e2e_value, e2e_steps, err_e2e = None, 0, None
+    else:
+        e2e_value, e2e_steps, err_e2e = run_e2e(D, torch, img, args, ws)
+
+    extras = {}
+    if not args.no_extras:
+        extras = run_extras(D, torch, stream, sptr)
+    sampler.stop()
+    clocks = sampler.summary(tw0, tw1)
+    
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = O.max_threads()
+        mpx, desc = cpu_baseline(img, threads)
+        cpu = {"value": round(mpx, 3), "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": "2D DWT throughput (CDF 9/7 forward+inverse, full depth)",
+            "value": round(value, 1), "unit": "Mpx/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 64-blob field + N(0,4) noise, integers 0..255)",
+            "config": {"workload": WORKLOAD, "image": [W, H], "j_max": J,
+                       "l2": "inputs (1 GiB) larger than L2, no flush",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": None if e2e_value is None else {"value": round(e2e_value, 1), "unit": "Mpx/s", "steps": e2e_steps,
+                    "h2d_bytes_per_step": 2 * W * H * 4, "d2h_bytes_per_step": 2 * W * H * 4,
+                    "api": "dwt_cdf97_2f_s + dwt_cdf97_2i_s on pinned host memory",
+                    "roundtrip_max_abs_err": err_e2e},
+            "roofline": {"bound": "hbm", "kernel": "level_kernel<4,false> (CDF 9/7 forward, level 0)",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                         "launch_ms": round(kms, 4)},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": args.steps * 2 * J,
+            "roundtrip_max_abs_err": err_rt,
+            "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(D, torch, img, args, ws):
+    """Forward + inverse through the drop-in C ABI on a pinned host image; the
+    calls copy the image in and the result out every time."""
+    host = torch.from_numpy(img.copy()).pin_memory()
+    hp = host.data_ptr()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        j = D.dwt_cdf97_2f_s(hp, W * 4, 4, W, H, W, H, J)
+        D.dwt_cdf97_2i_s(hp, W * 4, 4, W, H, W, H, j)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        j = D.dwt_cdf97_2f_s(hp, W * 4, 4, W, H, W, H, J)
+        D.dwt_cdf97_2i_s(hp, W * 4, 4, W, H, W, H, j)
+    e2e_s = allmax(ws, time.perf_counter() - t0)
+    e2e_value = ws * e2e_steps * 2 * W * H / e2e_s / 1e6
+    err_e2e = float(np.abs(host.numpy() - img).max())
+    return e2e_value, e2e_steps, err_e2e
+
+
+def run_extras(D, torch, stream, sptr):
+    """Secondary figures of the other configurations (outside the headline)."""
+    out = {}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    from libdwt_gb300 import synth
+    img = synth_image()
+    src = torch.from_numpy(img).cuda()
+    dst = torch.empty_like(src)
+    for wav in ("cdf97", "cdf53"):
+        for inv in (False, True):
+            ms = timed(lambda: D.transform2_dev(src, dst, wav, inv, J, 0, sptr), 10)
+            out[f"{wav}_{'inv' if inv else 'fwd'}_16384_mpx_s"] = round(W * H / ms / 1e3, 1)
+            out[f"{wav}_{'inv' if inv else 'fwd'}_16384_frac_alg"] = round(
+                2863311520 / (ms / 1e3) / 1e9 / hbm_peak()[0], 4)
+    # odd size: 16383 x 16385 (rows padded to a 16-byte pitch)
+    ow, oh = 16383, 16385
+    osrc = torch.zeros((oh, 16384), dtype=torch.float32, device="cuda")
+    osrc[:, :ow] = torch.from_numpy(synth.image(ow, oh, seed=1)).cuda()
+    odst = torch.empty((oh, ow), dtype=torch.float32, device="cuda")
+    for wav in ("cdf97", "cdf53"):
+        ms = timed(lambda: D.transform2_dev(osrc[:, :ow], odst, wav, False, J, 0, sptr), 10)
+        out[f"{wav}_fwd_16383x16385_mpx_s"] = round(ow * oh / ms / 1e3, 1)
+    del osrc, odst
+    # plain drop-in latency, 1024^2 j=5 on a host image (forward + inverse)
+    small = synth.image(1024, 1024, seed=2)
+    t = time.perf_counter()
+    n = 20
+    for _ in range(n):
+        j = D.dwt_cdf97_2f_s(small.ctypes.data, 4096, 4, 1024, 1024, 1024, 1024, 5)
+        D.dwt_cdf97_2i_s(small.ctypes.data, 4096, 4, 1024, 1024, 1024, 1024, j)
+    out["c0_1024_fwd_inv_host_ms"] = round((time.perf_counter() - t) / n * 1e3, 3)
+    dsmall = torch.from_numpy(small).cuda()
+
+    def c0dev():
+        j = D.dwt_cdf97_2f_s(dsmall.data_ptr(), 4096, 4, 1024, 1024, 1024, 1024, 5)
+        D.dwt_cdf97_2i_s(dsmall.data_ptr(), 4096, 4, 1024, 1024, 1024, 1024, j)
+    c0dev()
+    t = time.perf_counter()
+    for _ in range(n):
+        c0dev()
+    out["c0_1024_fwd_inv_device_ms"] = round((time.perf_counter() - t) / n * 1e3, 3)
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -147,6 +147,18 @@ DWT_EXPORT int dwt_gpu_2_dev(int wavelet, int inverse, const float *src, long lo
                   float *dst, long long dst_pitch_bytes, int w, int h, int j_levels,
                   int decompose_one, void *stream);
 
+/* One decomposition level, device-resident and out of place, enqueued on
+ * `stream`.  Forward: in[0] is the interleaved w x h image, out[0..3] receive
+ * LL, HL, LH, HH.  Inverse: in[0..3] are LL, HL, LH, HH of a w x h image,
+ * out[0] receives it.  Source pitches must be multiples of 16 bytes (and the
+ * forward source 16-byte aligned); destinations need 4-byte alignment. */
+DWT_EXPORT int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const float *const in[4],
+                                 const long long in_pitch_bytes[4], float *const out[4],
+                                 const long long out_pitch_bytes[4], void *stream);
+
+/* Waits for all device work and reports (and clears) a device-side error. */
+DWT_EXPORT int dwt_gpu_sync_check(void);
+
 /* Batched strided 1D level, in place, device or host memory: `count`
  * signals of N samples, signal s at base + (s / group) * group_stride +
  * (s % group) * lane_stride bytes, samples `stride` bytes apart; L to samples

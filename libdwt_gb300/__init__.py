@@ -54,6 +54,8 @@ def lib():
         L.dwt_gpu_1_s.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
         L.dwt_gpu_2_dev.argtypes = [_i, _i, _vp, _ll, _vp, _ll, _i, _i, _i, _i, _vp]
         L.dwt_gpu_1_batch_s.argtypes = [_i, _i, _vp, _i, _i, _ll, _i, _ll, _i]
+        L.dwt_gpu_level_dev.argtypes = [_i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_ll),
+                                        C.POINTER(_vp), C.POINTER(_ll), _vp]
         L.dwt_gpu_error_string.restype = C.c_char_p
         L.dwt_gpu_error_string.argtypes = [_i]
         L.dwt_util_set_accel.argtypes = [_i]
@@ -172,6 +174,18 @@ def transform2_dev(src, dst, wavelet, inverse: bool, j_levels: int = -1, decompo
     return _check(lib().dwt_gpu_2_dev(_WAVELETS[wavelet], 1 if inverse else 0, src.data_ptr(),
                                       src.stride(0) * 4, dst.data_ptr(), dst.stride(0) * 4, w, h,
                                       j_levels, decompose_one, stream))
+
+
+def level_dev(wavelet, inverse: bool, w: int, h: int, ins, in_pitch_bytes, outs,
+              out_pitch_bytes, stream: int = 0) -> None:
+    """One out-of-place level on device pointers (see dwt_gpu_level_dev)."""
+    def arr(t, vals):
+        vals = list(vals) + [0] * (4 - len(vals))
+        return (t * 4)(*vals)
+    _check(lib().dwt_gpu_level_dev(_WAVELETS[wavelet], 1 if inverse else 0, w, h,
+                                   arr(_vp, [_addr(x) for x in ins]), arr(_ll, in_pitch_bytes),
+                                   arr(_vp, [_addr(x) for x in outs]), arr(_ll, out_pitch_bytes),
+                                   stream))
 
 
 def strided_1d(wavelet, inverse: bool, a, b, c, d, N: int, stride: int) -> None:

@@ -303,15 +303,18 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     if (!in.p) return set_error(DWT_GPU_ENOMEM);
     Buf span;  // host path with a non-4-byte pixel pitch: device copy of the byte span
     const long long sb = span_bytes(sx, sy, ox, oy);
+    // 2D copies take rows of whole, 4-byte aligned floats; anything else goes
+    // through a byte span and the repack kernel
+    const bool rows4 = sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
     if (!on_device) {
-        if (sy == 4) {
+        if (rows4) {
             CK(cudaMemcpy2DAsync(in.p, P * 4, ptr, csx, size_t(ox) * 4, oy, cudaMemcpyHostToDevice, s));
         } else {
             if (!span.alloc(size_t(sb) + 16, s)) return set_error(DWT_GPU_ENOMEM);
             CK(cudaMemcpyAsync(span.p, ptr, size_t(sb), cudaMemcpyHostToDevice, s));
             CK(launch_repack(span.p, sx, sy, ox, oy, in.f(), P, s));
         }
-    } else if (sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0) {
+    } else if (rows4) {
         CK(cudaMemcpy2DAsync(in.p, P * 4, ptr, csx, size_t(ox) * 4, oy, cudaMemcpyDeviceToDevice, s));
     } else {
         CK(launch_repack(ptr, sx, sy, ox, oy, in.f(), P, s));
@@ -321,8 +324,7 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     float *out = nullptr;
     long long out_pitch = 0;
     Buf outb;
-    const bool direct = on_device && dense && sy == 4 && (csx % 4) == 0 &&
-                        (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
+    const bool direct = on_device && dense && rows4;
     if (dense) {
         if (direct) {
             out = static_cast<float *>(ptr);
@@ -366,7 +368,7 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
 
     // 3. write back
     if (!on_device) {
-        if (sy == 4) {
+        if (rows4) {
             CK(cudaMemcpy2DAsync(ptr, csx, out, out_pitch * 4, size_t(ox) * 4, oy, cudaMemcpyDeviceToHost, s));
         } else {
             CK(launch_unpack(out, out_pitch, span.p, sx, sy, ox, oy, s));
@@ -619,6 +621,45 @@ int dwt_gpu_1_batch_s(int wavelet, int inverse, void *base, int N, int stride, l
 {
     if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
     return run_1d_batch(wavelet, inverse != 0, base, N, stride, count, group, group_stride, lane_stride);
+}
+
+int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const float *const in[4],
+                      const long long in_pitch_bytes[4], float *const out[4],
+                      const long long out_pitch_bytes[4], void *stream)
+{
+    t_last_error = DWT_GPU_OK;
+    if ((wavelet != CDF97 && wavelet != CDF53) || w <= 0 || h <= 0 || !in || !out)
+        return set_error(DWT_GPU_EINVAL);
+    LevelDesc d{};
+    d.w = w;
+    d.h = h;
+    const int nin = inverse ? 4 : 1, nout = inverse ? 1 : 4;
+    for (int k = 0; k < nin; ++k) {
+        if (!in[k] || (in_pitch_bytes[k] % 16) != 0) return set_error(DWT_GPU_EINVAL);
+        d.in[k] = in[k];
+        d.in_pitch[k] = in_pitch_bytes[k] / 4;
+    }
+    if (!inverse && (reinterpret_cast<uintptr_t>(in[0]) & 15) != 0) return set_error(DWT_GPU_EINVAL);
+    for (int k = 0; k < nout; ++k) {
+        if (!out[k] || (out_pitch_bytes[k] % 4) != 0) return set_error(DWT_GPU_EINVAL);
+        d.out[k] = out[k];
+        d.out_pitch[k] = out_pitch_bytes[k] / 4;
+    }
+    plan_level(d, 0);
+    Context &c = ctx();
+    cudaError_t e = launch_level(d, wavelet, inverse != 0, static_cast<cudaStream_t>(stream), c.d_err);
+    if (e != cudaSuccess) {
+        log_error("CUDA error %s\n", cudaGetErrorString(e));
+        return set_error(DWT_GPU_ECUDA);
+    }
+    return DWT_GPU_OK;
+}
+
+int dwt_gpu_sync_check(void)
+{
+    Context &c = ctx();
+    if (cudaDeviceSynchronize() != cudaSuccess) return set_error(DWT_GPU_ECUDA);
+    return set_error(check_device_error(c));
 }
 
 void dwt_cdf97_2f_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,

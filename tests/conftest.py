@@ -43,6 +43,32 @@ class Golden:
         return self.arrays[case["id"] + "_in"], self.arrays[case["id"] + "_out"]
 
 
+def frame_equal(got: np.ndarray, exp: np.ndarray, sx: int, sy: int, ox: int, oy: int) -> bool:
+    """Bitwise equality of two byte buffers holding a float frame at byte
+    strides (sx, sy), except that two NaNs compare equal whatever their
+    payload (x86 and the GPU produce different default NaN bit patterns when
+    an overflowed input yields inf - inf).  Bytes outside the frame must be
+    identical."""
+    if np.array_equal(got, exp):
+        return True
+    diff = np.flatnonzero(got != exp)
+    ys, xs = np.meshgrid(np.arange(oy), np.arange(ox), indexing="ij")
+    starts = (ys * sx + xs * sy).ravel()
+    owner = {}
+    for k, s0 in enumerate(starts):
+        for b in range(4):
+            owner[int(s0) + b] = int(s0)
+    for d in diff:
+        s0 = owner.get(int(d))
+        if s0 is None:
+            return False
+        a = np.frombuffer(got[s0:s0 + 4].tobytes(), np.float32)[0]
+        b = np.frombuffer(exp[s0:s0 + 4].tobytes(), np.float32)[0]
+        if not (np.isnan(a) and np.isnan(b)):
+            return False
+    return True
+
+
 @pytest.fixture(scope="session")
 def golden():
     return Golden()
