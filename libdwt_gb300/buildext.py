@@ -17,10 +17,14 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
-LIB = os.path.join(LIBDIR, "libdwt_gb300.so")
+LIB = os.environ.get("DWT_GB300_LIB", os.path.join(LIBDIR, "libdwt_gb300.so"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+# --fmad=false: no multiply-add contraction anywhere.  The lifting must round
+# the product c*(l + r) before adding it, as the reference's float path does;
+# explicit .rn rounding alone did not keep packed f32x2 multiplies and adds
+# apart.
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 
 
@@ -47,9 +51,9 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _sources() + _headers() + [__file__])
 
 
-def _compile(src: str, verbose_ptxas: bool) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+def _compile(src: str, verbose_ptxas: bool, extra_flags=()) -> str:
+    obj = os.path.join(BUILD, os.path.basename(src) + "".join(extra_flags).replace("-", "_") + ".o")
+    cmd = [nvcc()] + NVCC_FLAGS + list(extra_flags) + ["-c", src, "-o", obj]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -60,15 +64,15 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     return obj
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> str:
+def build(force: bool = False, verbose_ptxas: bool = False, extra_flags=()) -> str:
     """Compile and link; returns the library path."""
     if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
+        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas, extra_flags), srcs))
     tmp = LIB + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -79,4 +83,5 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))
+    extra = [a for a in sys.argv[1:] if a.startswith("-D")]
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, extra_flags=extra))

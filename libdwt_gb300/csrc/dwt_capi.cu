@@ -23,6 +23,7 @@
 
 #include "../../include/libdwt.h"
 #include "dwt_capi_internal.h"
+#include "dwt_coarse.cuh"
 #include "dwt_generic.cuh"
 #include "dwt_level2d.cuh"
 
@@ -166,6 +167,14 @@ size_t dense_scratch_floats(int W, int H, int J, long long *pitch0, long long *p
     return n;
 }
 
+// First level whose LL band fits the single-CTA coarse kernel (J if none).
+static int coarse_level(int W, int H, int J)
+{
+    for (int j = 0; j < J; ++j)
+        if ((long long)ceil_div_pow2(W, j) * ceil_div_pow2(H, j) <= kCoarseMax) return j;
+    return J;
+}
+
 cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long long out_pitch, int W,
                           int H, int J, int wavelet, float *scratch, cudaStream_t s, int *err,
                           int seg_hint)
@@ -173,7 +182,8 @@ cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long 
     long long p[2];
     dense_scratch_floats(W, H, J, &p[0], &p[1]);
     float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
-    for (int j = 0; j < J; ++j) {
+    const int j0 = coarse_level(W, H, J);
+    for (int j = 0; j < j0; ++j) {
         const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
         const int wd = (w + 1) / 2, hd = (h + 1) / 2;
         LevelDesc d{};
@@ -196,6 +206,12 @@ cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long 
         cudaError_t e = launch_level(d, wavelet, false, s, err);
         if (e != cudaSuccess) return e;
     }
+    if (j0 < J) {
+        const float *src = j0 == 0 ? in : buf[(j0 - 1) % 2];
+        const long long sp = j0 == 0 ? in_pitch : p[(j0 - 1) % 2];
+        return launch_coarse(false, src, sp, ceil_div_pow2(W, j0), ceil_div_pow2(H, j0), J - j0, out,
+                             out_pitch, wavelet, s);
+    }
     return cudaSuccess;
 }
 
@@ -206,7 +222,17 @@ cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long 
     long long p[2];
     dense_scratch_floats(W, H, J, &p[0], &p[1]);
     float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
-    for (int j = J; j >= 1; --j) {
+    const int j0 = coarse_level(W, H, J);
+    int jtop = J;  // level whose LL the next level kernel reads
+    if (j0 < J) {
+        float *dst = j0 == 0 ? out : buf[(j0 - 1) % 2];
+        const long long dp = j0 == 0 ? out_pitch : p[(j0 - 1) % 2];
+        cudaError_t e = launch_coarse(true, in, in_pitch, ceil_div_pow2(W, j0), ceil_div_pow2(H, j0),
+                                      J - j0, dst, dp, wavelet, s);
+        if (e != cudaSuccess) return e;
+        jtop = j0;
+    }
+    for (int j = jtop; j >= 1; --j) {
         const int w = ceil_div_pow2(W, j - 1), h = ceil_div_pow2(H, j - 1);
         const int ws = (w + 1) / 2, hs = (h + 1) / 2;
         LevelDesc d{};

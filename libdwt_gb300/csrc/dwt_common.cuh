@@ -42,6 +42,53 @@ __device__ __forceinline__ float lift(float x, float c, float l, float r)
     return fadd(x, fmul(c, fadd(l, r)));
 }
 
+// Two floats in one 64-bit register pair.  Additions use the packed FP32x2
+// instruction of sm_100-class GPUs (add.rn.f32x2 rounds each half exactly as
+// add.rn.f32 does); multiplications stay scalar mul.rn.f32.  A packed
+// multiply that feeds a packed add is contracted into a fused multiply-add by
+// the code generator even with explicit .rn rounding and --fmad=false (one
+// rounding instead of two), which would break bit parity with the
+// reference; scalar mul.rn.f32 is never contracted.
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pk(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float f2lo(f2 v)
+{
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return a;
+}
+__device__ __forceinline__ float f2hi(f2 v)
+{
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    return b;
+}
+#ifndef DWT_SCALAR_PAIRS
+__device__ __forceinline__ f2 add2(f2 a, f2 b)
+{
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+#else
+__device__ __forceinline__ f2 add2(f2 a, f2 b)
+{
+    return pk(__fadd_rn(f2lo(a), f2lo(b)), __fadd_rn(f2hi(a), f2hi(b)));
+}
+#endif
+__device__ __forceinline__ f2 mul2(f2 a, f2 b)
+{
+    return pk(__fmul_rn(f2lo(a), f2lo(b)), __fmul_rn(f2hi(a), f2hi(b)));
+}
+// x + c*(l + r) on both halves
+__device__ __forceinline__ f2 lift2(f2 x, f2 c, f2 l, f2 r) { return add2(x, mul2(c, add2(l, r))); }
+
 // Whole-sample symmetric extension of index r into [0, n), n >= 2: the
 // periodic reflection with period 2(n-1).  Keeps the parity of r.
 __host__ __device__ __forceinline__ int mirror(int r, int n)

@@ -11,14 +11,15 @@ namespace dwt {
 // Work decomposition: a warp holds kStripIn interleaved columns of a row
 // (4 per lane) and produces the kStripOut middle ones; lanes 0 and 31 are the
 // lifting halo.  Rows are walked as (even, odd) pairs in segments of
-// seg_pairs output pairs, each segment warmed up by the lifting latency.
+// seg_pairs output pairs, each segment warmed up by the lifting latency;
+// one pipeline stage carries two pairs.
 constexpr int kLanes = 32;
 constexpr int kStripIn = 128;
 constexpr int kStripOut = 120;
 constexpr int kSlotF = 136;        // floats per forward row slot
 constexpr int kSlotI = 68;         // floats per inverse band-row slot
-constexpr int kStageFloats = 272;  // one pipeline stage = 2 rows or 4 band rows
-constexpr int kStages = 8;         // pipeline depth per warp
+constexpr int kStageFloats = 544;  // one pipeline stage = 2 row pairs: 4 rows or 8 band rows
+constexpr int kStages = 4;         // pipeline depth per warp (8 row pairs)
 constexpr int kWarpsPerCta = 4;
 constexpr int kSmemBytes = kWarpsPerCta * (kStages * kStageFloats * 4 + kStages * 8);
 
