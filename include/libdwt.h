@@ -159,6 +159,20 @@ DWT_EXPORT int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const f
 /* Waits for all device work and reports (and clears) a device-side error. */
 DWT_EXPORT int dwt_gpu_sync_check(void);
 
+/* No counterpart in the reference.  dwt_gpu_2_dev without any device
+ * allocation, for callers that may not allocate device memory: plugins whose
+ * host application owns every device allocation, services that budget every
+ * byte, and latency-critical loops that cannot risk cudaMalloc/cudaFree (which
+ * may synchronize the device).  Its inter-level scratch is a fixed ~5.2 MB
+ * array inside the library (held by every GPU that loads it, until exit);
+ * images up to 2048 x 2048 fit, larger ones return DWT_GPU_EINVAL.  The first
+ * call on a device looks the array up (make it before any stream capture).
+ * All calls share the array: calls whose GPU work overlaps race. */
+DWT_EXPORT int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
+                                     long long src_pitch_bytes, float *dst,
+                                     long long dst_pitch_bytes, int w, int h, int j_levels,
+                                     int decompose_one, void *stream);
+
 /* Batched strided 1D level, in place, device or host memory: `count`
  * signals of N samples, signal s at base + (s / group) * group_stride +
  * (s % group) * lane_stride bytes, samples `stride` bytes apart; L to samples
