@@ -171,7 +171,7 @@ size_t dense_scratch_floats(int W, int H, int J, long long *pitch0, long long *p
 static int coarse_level(int W, int H, int J)
 {
     for (int j = 0; j < J; ++j)
-        if ((long long)ceil_div_pow2(W, j) * ceil_div_pow2(H, j) <= kCoarseMax) return j;
+        if (coarse_fits(ceil_div_pow2(W, j), ceil_div_pow2(H, j))) return j;
     return J;
 }
 

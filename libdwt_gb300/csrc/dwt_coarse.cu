@@ -1,14 +1,16 @@
 // All remaining coarse levels of one image in a single CTA.
 //
-// Once the LL band is small (at most kCoarseMax samples), each further level
-// has too little work to fill the GPU and a launch per level costs more than
-// the level itself.  This kernel loads the band into shared memory and runs
-// every remaining level there: per level a row pass and a column pass, each
-// as parallel lifting sweeps (one __syncthreads per sweep) with the same
-// per-sample arithmetic as the reference (x + c*(l + r), symmetric
-// extension, scaling), then deinterleaves into the second buffer.  The
-// forward writes each level's detail bands and the final LL to the output
-// frame; the inverse reads them and writes the reconstructed band.
+// Once the LL band is small, each further level has too little work to fill
+// the GPU and a launch per level costs more than the level itself.  This
+// kernel loads the band into shared memory and runs every remaining level
+// there.  A pass gives each line (row or column) to one warp, which holds up
+// to 256 samples in registers (8 per lane, mirrored past the end of the
+// line) and runs the lifting steps with warp shuffles, the same per-sample
+// arithmetic as the reference (x + c*(l + r), symmetric extension, scaling).
+// Each pass writes its result transposed and deinterleaved into the other
+// buffer, so the column pass reads its lines as rows too.  The forward writes
+// each level's detail bands and the final LL to the output frame; the
+// inverse reads them and writes the reconstructed band.
 #include "dwt_coarse.cuh"
 
 #include <algorithm>
@@ -18,116 +20,157 @@ namespace dwt {
 namespace {
 
 constexpr int kThreads = 1024;
+constexpr int kWarps = kThreads / 32;
+constexpr int kV = 8;  // samples per lane: one warp holds 256 samples of a line
+constexpr unsigned kAll = 0xffffffffu;
 
-// One lifting step on samples of `parity` of `nl` lines of length n:
-// line l, sample i at buf[l*ls + i*es].  Consecutive threads take
-// consecutive lines when lines are adjacent in memory (ls == 1, the column
-// pass) and consecutive samples otherwise, so shared-memory accesses of a
-// warp spread over the banks.
-__device__ __forceinline__ void sweep(float *buf, int ls, int es, int nl, int n, int parity, float c)
+// Forward lifting of one line of length n (2 <= n <= 252) held by a warp,
+// sample 8*lane + k in x[k]; samples past the end hold their mirror images.
+// Every lifting step is applied uniformly; the left neighbour of sample 0 is
+// sample 1 (symmetric extension), and the missing right neighbour of the
+// warp's last sample only disturbs samples >= 252 - 4 steps, beyond n + 3.
+template <int NS>
+__device__ __forceinline__ void line_forward(float x[kV], const Wavelet &W, int lane)
 {
-    const int half = (n - parity + 1) >> 1;  // samples of this parity
-    const int tot = nl * half;
-    for (int k = threadIdx.x; k < tot; k += blockDim.x) {
-        int l, j;
-        if (ls == 1) {
-            j = k / nl;
-            l = k - j * nl;
-        } else {
-            l = k / half;
-            j = k - l * half;
-        }
-        const int i = parity + 2 * j;
-        float *x = buf + l * ls;
-        const float left = (i > 0) ? x[(i - 1) * es] : x[(i + 1) * es];
-        const float right = (i + 1 < n) ? x[(i + 1) * es] : x[(i - 1) * es];
-        x[i * es] = lift(x[i * es], c, left, right);
+#pragma unroll
+    for (int s = 0; s < NS; s += 2) {
+        const float nx = __shfl_down_sync(kAll, x[0], 1);
+#pragma unroll
+        for (int k = 1; k < kV - 1; k += 2) x[k] = lift(x[k], W.c[s], x[k - 1], x[k + 1]);
+        x[kV - 1] = lift(x[kV - 1], W.c[s], x[kV - 2], nx);
+        float pv = __shfl_up_sync(kAll, x[kV - 1], 1);
+        if (lane == 0) pv = x[1];
+        x[0] = lift(x[0], W.c[s + 1], pv, x[1]);
+#pragma unroll
+        for (int k = 2; k < kV; k += 2) x[k] = lift(x[k], W.c[s + 1], x[k - 1], x[k + 1]);
+    }
+#pragma unroll
+    for (int k = 0; k < kV; ++k) x[k] = fmul(x[k], (k & 1) ? W.zeta_o : W.zeta_e);
+}
+
+template <int NS>
+__device__ __forceinline__ void line_inverse(float x[kV], const Wavelet &W, int lane)
+{
+#pragma unroll
+    for (int k = 0; k < kV; ++k) x[k] = fmul(x[k], (k & 1) ? W.zeta_e : W.zeta_o);
+#pragma unroll
+    for (int s = 0; s < NS; s += 2) {
+        float pv = __shfl_up_sync(kAll, x[kV - 1], 1);
+        if (lane == 0) pv = x[1];
+        x[0] = lift(x[0], W.c[s], pv, x[1]);
+#pragma unroll
+        for (int k = 2; k < kV; k += 2) x[k] = lift(x[k], W.c[s], x[k - 1], x[k + 1]);
+        const float nx = __shfl_down_sync(kAll, x[0], 1);
+#pragma unroll
+        for (int k = 1; k < kV - 1; k += 2) x[k] = lift(x[k], W.c[s + 1], x[k - 1], x[k + 1]);
+        x[kV - 1] = lift(x[kV - 1], W.c[s + 1], x[kV - 2], nx);
     }
 }
 
-// Forward lifting of nl lines of length n >= 2 in place (no scaling).
-__device__ __forceinline__ void lines_lift_fwd(float *buf, int ls, int es, int nl, int n, const Wavelet &W)
+// One forward pass over `nl` lines of length n: line l sample i read from
+// src[l*ls + i]; results deinterleaved and transposed into dst: sample i of
+// line l goes to dst[(i even ? i/2 : nd + i/2) * dp + l], nd = ceil(n/2).
+// The lane's mirrored load offsets and store rows depend only on n, so they
+// are computed once per pass.
+template <int NS>
+__device__ __forceinline__ void pass_forward(const float *src, int ls, float *dst, int dp, int nl, int n,
+                                             const Wavelet &W, int warp, int lane)
 {
-    for (int s = 0; s < W.nsteps; ++s) {
-        sweep(buf, ls, es, nl, n, (s & 1) ? 0 : 1, W.c[s]);
-        __syncthreads();
+    const int nd = (n + 1) >> 1;
+    if (n == 1) {
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) dst[l] = fmul(src[l * ls], W.n1_fwd);
+        return;
+    }
+    int ld[kV], st[kV];
+#pragma unroll
+    for (int k = 0; k < kV; ++k) {
+        const int i = kV * lane + k;
+        ld[k] = mirror(i, n);
+        st[k] = i < n ? ((k & 1) ? nd + (i >> 1) : (i >> 1)) * dp : -1;
+    }
+    for (int l = warp; l < nl; l += kWarps) {
+        const float *line = src + l * ls;
+        float x[kV];
+#pragma unroll
+        for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+        line_forward<NS>(x, W, lane);
+#pragma unroll
+        for (int k = 0; k < kV; ++k)
+            if (st[k] >= 0) dst[st[k] + l] = x[k];
     }
 }
 
-__device__ __forceinline__ void lines_lift_inv(float *buf, int ls, int es, int nl, int n, const Wavelet &W)
+// One inverse pass: line l holds L samples at src[l*ls + j] (j < nd) and H
+// samples at src[l*ls + nd + j]; rebuilt samples transposed into dst[i*dp + l].
+template <int NS>
+__device__ __forceinline__ void pass_inverse(const float *src, int ls, float *dst, int dp, int nl, int n,
+                                             const Wavelet &W, int warp, int lane)
 {
-    for (int s = 0; s < W.nsteps; ++s) {
-        sweep(buf, ls, es, nl, n, (s & 1) ? 1 : 0, W.c[s]);
-        __syncthreads();
+    const int nd = (n + 1) >> 1;
+    if (n == 1) {
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) dst[l] = fmul(src[l * ls], W.n1_inv);
+        return;
+    }
+    int ld[kV], st[kV];
+#pragma unroll
+    for (int k = 0; k < kV; ++k) {
+        const int i = kV * lane + k;
+        const int m = mirror(i, n);
+        ld[k] = (m & 1) ? nd + (m >> 1) : (m >> 1);
+        st[k] = i < n ? i * dp : -1;
+    }
+    for (int l = warp; l < nl; l += kWarps) {
+        const float *line = src + l * ls;
+        float x[kV];
+#pragma unroll
+        for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+        line_inverse<NS>(x, W, lane);
+#pragma unroll
+        for (int k = 0; k < kV; ++k)
+            if (st[k] >= 0) dst[st[k] + l] = x[k];
     }
 }
 
+// A: the band, row-major with pitch P; B: its transpose, pitch PT.
+template <int NS>
 __global__ void __launch_bounds__(kThreads)
 coarse_forward_kernel(const float *in, long long in_pitch, int w0, int h0, int levels, float *out,
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ float sm[];
-    const int P = w0;
+    const int P = w0 + 1, PT = h0 + 1;
     float *A = sm, *B = sm + P * h0;
-    for (int k = threadIdx.x; k < w0 * h0; k += blockDim.x) {
-        const int y = k / w0, x = k - y * w0;
-        A[y * P + x] = in[y * in_pitch + x];
-    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
+        for (int x = threadIdx.x & 31; x < w0; x += 32) A[y * P + x] = in[y * in_pitch + x];
     __syncthreads();
     int w = w0, h = h0;
     for (int lvl = 0; lvl < levels; ++lvl) {
         const int wd = (w + 1) >> 1, hd = (h + 1) >> 1;
-        // rows y < h, length w: lift in A, then scale + deinterleave into B
-        if (w > 1) lines_lift_fwd(A, P, 1, h, w, W);
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int y = k / w, x = k - y * w;
-            const float v = A[y * P + x];
-            if (w == 1)
-                B[y * P] = fmul(v, W.n1_fwd);
-            else if ((x & 1) == 0)
-                B[y * P + (x >> 1)] = fmul(v, W.zeta_e);
-            else
-                B[y * P + wd + (x >> 1)] = fmul(v, W.zeta_o);
-        }
+        pass_forward<NS>(A, P, B, PT, h, w, W, warp, lane);  // rows -> columns of B
         __syncthreads();
-        // columns x < w, length h: lift in B, then scale + deinterleave into A
-        if (h > 1) lines_lift_fwd(B, 1, P, w, h, W);
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int y = k / w, x = k - y * w;
-            const float v = B[y * P + x];
-            if (h == 1)
-                A[x] = fmul(v, W.n1_fwd);
-            else if ((y & 1) == 0)
-                A[(y >> 1) * P + x] = fmul(v, W.zeta_e);
-            else
-                A[(hd + (y >> 1)) * P + x] = fmul(v, W.zeta_o);
-        }
+        pass_forward<NS>(B, PT, A, P, w, h, W, warp, lane);  // columns -> rows of A
         __syncthreads();
-        // this level's detail bands are final
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int y = k / w, x = k - y * w;
-            if (x >= wd || y >= hd) out[y * out_pitch + x] = A[y * P + x];
-        }
+        for (int y = warp; y < h; y += kWarps)
+            for (int x = (y < hd ? wd : 0) + lane; x < w; x += 32) out[y * out_pitch + x] = A[y * P + x];
         w = wd;
         h = hd;
     }
-    for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-        const int y = k / w, x = k - y * w;
-        out[y * out_pitch + x] = A[y * P + x];
-    }
+    for (int y = warp; y < h; y += kWarps)
+        for (int x = lane; x < w; x += 32) out[y * out_pitch + x] = A[y * P + x];
 }
 
+template <int NS>
 __global__ void __launch_bounds__(kThreads)
 coarse_inverse_kernel(const float *in, long long in_pitch, int w0, int h0, int levels, float *out,
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ float sm[];
-    const int P = w0;
+    const int P = w0 + 1, PT = h0 + 1;
     float *A = sm, *B = sm + P * h0;
-    for (int k = threadIdx.x; k < w0 * h0; k += blockDim.x) {
-        const int y = k / w0, x = k - y * w0;
-        A[y * P + x] = in[y * in_pitch + x];
-    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
+        for (int x = threadIdx.x & 31; x < w0; x += 32) A[y * P + x] = in[y * in_pitch + x];
     __syncthreads();
     for (int lvl = levels - 1; lvl >= 0; --lvl) {
         int w = w0, h = h0;
@@ -135,44 +178,21 @@ coarse_inverse_kernel(const float *in, long long in_pitch, int w0, int h0, int l
             w = (w + 1) >> 1;
             h = (h + 1) >> 1;
         }
-        const int ws = (w + 1) >> 1, hs = (h + 1) >> 1;
-        // rows y < h: interleave L (cols < ws) and H (cols >= ws) into B with
-        // the pre-scaling, then lift (src/libdwt.c:5806-5811)
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int y = k / w, x = k - y * w;
-            if (w == 1)
-                B[y * P] = fmul(A[y * P], W.n1_inv);
-            else if ((x & 1) == 0)
-                B[y * P + x] = fmul(A[y * P + (x >> 1)], W.zeta_o);
-            else
-                B[y * P + x] = fmul(A[y * P + ws + (x >> 1)], W.zeta_e);
-        }
+        // rows first (src/libdwt.c:6706-6717): rows of A -> columns of B
+        pass_inverse<NS>(A, P, B, PT, h, w, W, warp, lane);
         __syncthreads();
-        if (w > 1) lines_lift_inv(B, P, 1, h, w, W);
-        // columns x < w: interleave L rows and H rows into A, pre-scale, lift
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int y = k / w, x = k - y * w;
-            if (h == 1)
-                A[x] = fmul(B[x], W.n1_inv);
-            else if ((y & 1) == 0)
-                A[y * P + x] = fmul(B[(y >> 1) * P + x], W.zeta_o);
-            else
-                A[y * P + x] = fmul(B[(hs + (y >> 1)) * P + x], W.zeta_e);
-        }
+        // then columns: columns of B hold the L rows then the H rows
+        pass_inverse<NS>(B, PT, A, P, w, h, W, warp, lane);
         __syncthreads();
-        if (h > 1) lines_lift_inv(A, 1, P, w, h, W);
     }
-    for (int k = threadIdx.x; k < w0 * h0; k += blockDim.x) {
-        const int y = k / w0, x = k - y * w0;
-        out[y * out_pitch + x] = A[y * P + x];
-    }
+    for (int y = warp; y < h0; y += kWarps)
+        for (int x = lane; x < w0; x += 32) out[y * out_pitch + x] = A[y * P + x];
 }
 
 template <typename K>
 cudaError_t configure(K kernel)
 {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                2 * kCoarseMax * 4);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kCoarseSmem);
 }
 
 }  // namespace
@@ -182,18 +202,27 @@ cudaError_t launch_coarse(bool inverse, const float *in, long long in_pitch, int
 {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = configure(coarse_forward_kernel);
-        if (e == cudaSuccess) e = configure(coarse_inverse_kernel);
+        cudaError_t e = configure(coarse_forward_kernel<4>);
+        if (e == cudaSuccess) e = configure(coarse_inverse_kernel<4>);
+        if (e == cudaSuccess) e = configure(coarse_forward_kernel<2>);
+        if (e == cudaSuccess) e = configure(coarse_inverse_kernel<2>);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    if ((long long)w * h > kCoarseMax || w <= 0 || h <= 0) return cudaErrorInvalidValue;
+    if (!coarse_fits(w, h)) return cudaErrorInvalidValue;
     const Wavelet W = make_wavelet(wavelet, inverse);
-    const size_t smem = size_t(2) * w * h * 4;
-    if (inverse)
-        coarse_inverse_kernel<<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
-    else
-        coarse_forward_kernel<<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+    const size_t smem = size_t(4) * ((w + 1) * h + (h + 1) * w);
+    if (wavelet == CDF97) {
+        if (inverse)
+            coarse_inverse_kernel<4><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+        else
+            coarse_forward_kernel<4><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+    } else {
+        if (inverse)
+            coarse_inverse_kernel<2><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+        else
+            coarse_forward_kernel<2><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+    }
     return cudaGetLastError();
 }
 

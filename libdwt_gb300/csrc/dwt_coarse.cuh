@@ -5,9 +5,16 @@
 
 namespace dwt {
 
-// Largest band (w * h samples) the coarse kernel takes: two float buffers of
-// this size live in shared memory.
-constexpr int kCoarseMax = 16384;
+// Shared memory of the coarse kernel: the band (pitch w+1) and its
+// transpose (pitch h+1).
+constexpr int kCoarseSmem = 200 * 1024;
+// Bands the coarse kernel takes: lines of at most 252 samples (one warp), and
+// both buffers within kCoarseSmem.
+__host__ __device__ inline bool coarse_fits(int w, int h)
+{
+    return w >= 1 && h >= 1 && w <= 252 && h <= 252 &&
+           4LL * ((long long)(w + 1) * h + (long long)(h + 1) * w) <= kCoarseSmem;
+}
 
 // Forward: `in` is the w x h LL band entering level j0; runs `levels` levels
 // and writes every detail band plus the final LL into the w x h top-left
