@@ -182,6 +182,48 @@ DWT_EXPORT int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
 DWT_EXPORT int dwt_gpu_1_batch_s(int wavelet, int inverse, void *base, int N, int stride, long long count,
                       int group, long long group_stride, int lane_stride);
 
+/* ------------------------------------------------------------- batches */
+
+/* One image of a batch: device frames, out of place (src rows 16-byte
+ * aligned), a w x h dense image, j_levels < 0 for the full depth, wavelet
+ * DWT_GPU_CDF97 / DWT_GPU_CDF53, inverse 0 / 1. */
+typedef struct {
+    const float *src;
+    long long src_pitch_bytes;
+    float *dst;
+    long long dst_pitch_bytes;
+    int w, h;
+    int j_levels;
+    int decompose_one;
+    int wavelet;
+    int inverse;
+} dwt_gpu_batch_image;
+
+/* Tunables of the batched kernel: rows pairs per work unit (tile height),
+ * side of the band from which one warp runs all remaining levels (the
+ * fused-level depth; 0 = none), resident CTAs per SM. */
+typedef struct {
+    int seg_pairs;
+    int tail_side;
+    int ctas_per_sm;
+} dwt_gpu_batch_params;
+
+typedef struct dwt_gpu_batch dwt_gpu_batch;
+
+/* Plans a batch: descriptors, work queue, scratch, and a CUDA graph of one
+ * persistent launch.  params = NULL runs the autotuner (times candidate
+ * settings on this batch, caches the winner by batch signature in
+ * $DWT_GPU_TUNE_CACHE or ~/.cache/libdwt_gb300_batch_tune.txt).  While
+ * tuning, dst frames are written. */
+DWT_EXPORT int dwt_gpu_batch_create(dwt_gpu_batch **out, int n, const dwt_gpu_batch_image *images,
+                                    const dwt_gpu_batch_params *params);
+/* Replays the batch's graph on `stream` (asynchronous). */
+DWT_EXPORT int dwt_gpu_batch_run(dwt_gpu_batch *b, void *stream);
+DWT_EXPORT int dwt_gpu_batch_params_get(const dwt_gpu_batch *b, dwt_gpu_batch_params *p);
+/* Work items of the planned batch. */
+DWT_EXPORT int dwt_gpu_batch_items(const dwt_gpu_batch *b);
+DWT_EXPORT void dwt_gpu_batch_destroy(dwt_gpu_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

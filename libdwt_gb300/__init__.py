@@ -33,6 +33,18 @@ class DwtError(RuntimeError):
     pass
 
 
+class BatchImage(C.Structure):
+    """dwt_gpu_batch_image (include/libdwt.h)."""
+    _fields_ = [("src", _vp), ("src_pitch_bytes", _ll), ("dst", _vp), ("dst_pitch_bytes", _ll),
+                ("w", _i), ("h", _i), ("j_levels", _i), ("decompose_one", _i), ("wavelet", _i),
+                ("inverse", _i)]
+
+
+class BatchParams(C.Structure):
+    """dwt_gpu_batch_params (include/libdwt.h)."""
+    _fields_ = [("seg_pairs", _i), ("tail_side", _i), ("ctas_per_sm", _i)]
+
+
 _lib = None
 
 
@@ -56,6 +68,13 @@ def lib():
         L.dwt_gpu_1_batch_s.argtypes = [_i, _i, _vp, _i, _i, _ll, _i, _ll, _i]
         L.dwt_gpu_level_dev.argtypes = [_i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_ll),
                                         C.POINTER(_vp), C.POINTER(_ll), _vp]
+        L.dwt_gpu_batch_create.argtypes = [C.POINTER(C.c_void_p), _i, C.POINTER(BatchImage),
+                                           C.POINTER(BatchParams)]
+        L.dwt_gpu_batch_run.argtypes = [C.c_void_p, _vp]
+        L.dwt_gpu_batch_params_get.argtypes = [C.c_void_p, C.POINTER(BatchParams)]
+        L.dwt_gpu_batch_items.argtypes = [C.c_void_p]
+        L.dwt_gpu_batch_destroy.argtypes = [C.c_void_p]
+        L.dwt_gpu_sync_check.restype = _i
         L.dwt_gpu_error_string.restype = C.c_char_p
         L.dwt_gpu_error_string.argtypes = [_i]
         L.dwt_util_set_accel.argtypes = [_i]
@@ -200,3 +219,49 @@ def batch_1d(wavelet, inverse: bool, base, N: int, stride: int, count: int, grou
     """Batched in-place strided 1D level over a bank of signals."""
     _check(lib().dwt_gpu_1_batch_s(_WAVELETS[wavelet], 1 if inverse else 0, _addr(base), N, stride,
                                    count, group, group_stride, lane_stride))
+
+
+class Batch:
+    """A planned batch of device-resident images (dwt_gpu_batch_*).
+
+    images: list of dicts with src, dst (torch CUDA tensors, 2D float32; src
+    rows 16-byte aligned), wavelet, inverse, j_levels (default -1).
+    params: (seg_pairs, tail_side, ctas_per_sm) or None to autotune."""
+
+    def __init__(self, images, params=None):
+        L = lib()
+        arr = (BatchImage * len(images))()
+        for k, im in enumerate(images):
+            src, dst = im["src"], im["dst"]
+            h, w = dst.shape
+            arr[k] = BatchImage(src.data_ptr(), src.stride(0) * 4, dst.data_ptr(), dst.stride(0) * 4, w, h,
+                                im.get("j_levels", -1), im.get("decompose_one", 0),
+                                _WAVELETS[im["wavelet"]], 1 if im.get("inverse") else 0)
+        self._keep = images
+        self._h = C.c_void_p()
+        p = None if params is None else C.byref(BatchParams(*params))
+        _check(L.dwt_gpu_batch_create(C.byref(self._h), len(images), arr, p))
+
+    def run(self, stream: int = 0) -> None:
+        _check(lib().dwt_gpu_batch_run(self._h, stream))
+
+    @property
+    def params(self):
+        p = BatchParams()
+        _check(lib().dwt_gpu_batch_params_get(self._h, C.byref(p)))
+        return (p.seg_pairs, p.tail_side, p.ctas_per_sm)
+
+    @property
+    def items(self) -> int:
+        return lib().dwt_gpu_batch_items(self._h)
+
+    def close(self) -> None:
+        if self._h:
+            lib().dwt_gpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

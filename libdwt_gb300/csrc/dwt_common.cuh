@@ -30,7 +30,48 @@ struct Wavelet {
 
 enum WaveletId { CDF97 = 0, CDF53 = 1 };
 
-// Host-side construction (float arithmetic on the host matches the device).
+// The parameters of wavelet `id` (CDF97 / CDF53) for one direction.  Usable
+// on the host and in device code; 1/zeta is a correctly rounded float
+// division in both.
+__host__ __device__ inline Wavelet make_wavelet_dev(int id, bool inverse)
+{
+    Wavelet w{};
+    if (id == CDF97) {
+        // src/libdwt.c:541-547
+        const float p1 = 1.58613434342059f, u1 = -0.0529801185729f;
+        const float p2 = -0.8829110755309f, u2 = 0.4435068520439f;
+        const float s1 = 1.1496043988602f;
+        const float s2 = (float)(1 / 1.1496043988602);
+        w.nsteps = 4;
+        w.zeta_e = s1;
+        w.zeta_o = 1.0f / s1;
+        w.n1_fwd = s1;
+        w.n1_inv = s2;
+        if (!inverse) {
+            w.c[0] = -p1; w.c[1] = u1; w.c[2] = -p2; w.c[3] = u2;
+        } else {
+            w.c[0] = -u2; w.c[1] = p2; w.c[2] = -u1; w.c[3] = p1;
+        }
+    } else {
+        // src/libdwt.c:566-569
+        const float p1 = 0.5f, u1 = 0.25f;
+        const float s1 = (float)1.41421356237309504880, s2 = (float)0.70710678118654752440;
+        w.nsteps = 2;
+        w.zeta_e = s1;
+        w.zeta_o = s2;
+        w.n1_fwd = s1;
+        w.n1_inv = s2;
+        if (!inverse) {
+            w.c[0] = -p1; w.c[1] = u1;
+        } else {
+            w.c[0] = -u1; w.c[1] = p1;
+        }
+        w.c[2] = w.c[3] = 0.0f;
+    }
+    return w;
+}
+
+// Host-side construction for kernel launches.
 Wavelet make_wavelet(int id, bool inverse);
 
 // Exact IEEE single operations that the compiler may not fuse into an FMA.

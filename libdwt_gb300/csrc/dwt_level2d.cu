@@ -1,25 +1,8 @@
-// Fused row + column lifting level for GB300 (sm_103a).
-//
-// Each warp owns one work unit: a strip of 128 interleaved columns (4 per
-// lane) by a segment of row pairs.  Its rows (forward) or band rows (inverse)
-// are streamed into a private shared-memory ring by the TMA bulk-copy engine
-// (cp.async.bulk + mbarrier complete_tx), one stage per row pair, kStages
-// stages deep.  For every row pair the warp
-//   1. reads its 4 columns of each row from shared memory,
-//   2. runs the horizontal lifting steps in registers, exchanging the one
-//      neighbour value per step with warp shuffles,
-//   3. advances the vertical lifting as a per-column register recurrence that
-//      emits one finished output row pair per input row pair, and
-//   4. stores the finished pair with coalesced vector stores.
-// Symmetric extension at the image borders is applied by reading mirrored
-// columns (lane offsets) and mirrored rows (the producer's row choice), which
-// reproduces the reference's boundary formulas bit for bit
-// (accel_lift_op4s_prolog_s / _epilog_s / _short_s, src/libdwt.c:5036-5377).
-//
-// Arithmetic follows the reference's float path operation by operation
-// (x + c*(l + r) with three roundings, scaling afterwards / beforehand), so
-// every output equals the reference's to the last bit.
+// Fused row + column lifting level for GB300 (sm_103a): the per-level kernel
+// over the warp work units of dwt_units.cuh, the level planner and the
+// wavelet constants.
 #include "dwt_level2d.cuh"
+#include "dwt_units.cuh"
 
 #include <algorithm>
 
@@ -27,768 +10,16 @@ namespace dwt {
 
 Wavelet make_wavelet(int id, bool inverse)
 {
-    Wavelet w{};
-    if (id == CDF97) {
-        // src/libdwt.c:541-547
-        const float p1 = 1.58613434342059f, u1 = -0.0529801185729f;
-        const float p2 = -0.8829110755309f, u2 = 0.4435068520439f;
-        const float s1 = 1.1496043988602f;
-        const float s2 = (float)(1 / 1.1496043988602);
-        volatile float one = 1.0f;  // 1/zeta as a float division, as the reference computes it
-        w.nsteps = 4;
-        w.zeta_e = s1;
-        w.zeta_o = one / s1;
-        w.n1_fwd = s1;
-        w.n1_inv = s2;
-        if (!inverse) {
-            w.c[0] = -p1; w.c[1] = u1; w.c[2] = -p2; w.c[3] = u2;
-        } else {
-            w.c[0] = -u2; w.c[1] = p2; w.c[2] = -u1; w.c[3] = p1;
-        }
-    } else {
-        // src/libdwt.c:566-569
-        const float p1 = 0.5f, u1 = 0.25f;
-        const float s1 = (float)1.41421356237309504880, s2 = (float)0.70710678118654752440;
-        w.nsteps = 2;
-        w.zeta_e = s1;
-        w.zeta_o = s2;
-        w.n1_fwd = s1;
-        w.n1_inv = s2;
-        if (!inverse) {
-            w.c[0] = -p1; w.c[1] = u1;
-        } else {
-            w.c[0] = -u1; w.c[1] = p1;
-        }
-        w.c[2] = w.c[3] = 0.0f;
-    }
-    return w;
+    const Wavelet w = make_wavelet_dev(id, inverse);
+    // 1/zeta must be the float division 1.0f / s1 (src/libdwt.c:1637-1640),
+    // one ulp away from the separately rounded constant s2
+    volatile float one = 1.0f;
+    Wavelet r = w;
+    if (id == CDF97) r.zeta_o = one / w.zeta_e;
+    return r;
 }
 
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
-
-// Forward horizontal lifting of the lane's 4 interleaved samples
-// (even, odd, even, odd), neighbours from lanes l-1 / l+1.
-template <int NS>
-__device__ __forceinline__ void h_forward(float v[4], const Wavelet &W)
-{
-#pragma unroll
-    for (int s = 0; s < NS; s += 2) {
-        const float nx = __shfl_down_sync(kFull, v[0], 1);
-        v[1] = lift(v[1], W.c[s], v[0], v[2]);
-        v[3] = lift(v[3], W.c[s], v[2], nx);
-        const float pv = __shfl_up_sync(kFull, v[3], 1);
-        v[0] = lift(v[0], W.c[s + 1], pv, v[1]);
-        v[2] = lift(v[2], W.c[s + 1], v[1], v[3]);
-    }
-    v[0] = fmul(v[0], W.zeta_e);
-    v[1] = fmul(v[1], W.zeta_o);
-    v[2] = fmul(v[2], W.zeta_e);
-    v[3] = fmul(v[3], W.zeta_o);
-}
-
-template <int NS>
-__device__ __forceinline__ void h_inverse(float v[4], const Wavelet &W)
-{
-    v[0] = fmul(v[0], W.zeta_o);
-    v[1] = fmul(v[1], W.zeta_e);
-    v[2] = fmul(v[2], W.zeta_o);
-    v[3] = fmul(v[3], W.zeta_e);
-#pragma unroll
-    for (int s = 0; s < NS; s += 2) {
-        const float pv = __shfl_up_sync(kFull, v[3], 1);
-        v[0] = lift(v[0], W.c[s], pv, v[1]);
-        v[2] = lift(v[2], W.c[s], v[1], v[3]);
-        const float nx = __shfl_down_sync(kFull, v[0], 1);
-        v[1] = lift(v[1], W.c[s + 1], v[0], v[2]);
-        v[3] = lift(v[3], W.c[s + 1], v[2], nx);
-    }
-}
-
-__device__ __forceinline__ void store4(float *p, const float v[4], const bool ok[4])
-{
-    if (ok[0] && ok[1] && ok[2] && ok[3] && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
-        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
-    } else {
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-            if (ok[i]) p[i] = v[i];
-    }
-}
-
-__device__ __forceinline__ void raise_error(int *err, int code)
-{
-    if (err) atomicCAS(err, 0, code);
-}
-
-// Stage ring cursor: stage index and mbarrier phase parity, advanced per use.
-struct Cursor {
-    uint32_t st, par;
-    __device__ __forceinline__ void next()
-    {
-        if (++st == kStages) {
-            st = 0;
-            par ^= 1u;
-        }
-    }
-};
-
-__device__ __forceinline__ Cursor cursor_at(uint32_t tick)
-{
-    return Cursor{tick % kStages, (tick / kStages) & 1u};
-}
-
-// Row pair m of a column of height h: the two source rows, mirrored only at
-// the image borders.
-__device__ __forceinline__ void pair_rows(int m, int h, int &ra, int &rb)
-{
-    ra = 2 * m;
-    rb = ra + 1;
-    if (ra < 0 || rb >= h) {
-        ra = mirror(2 * m, h);
-        rb = mirror(2 * m + 1, h);
-    }
-}
-
-// Per-lane store pointer for one band row stream: base + column, advanced by
-// the pitch per output row; vector stores when the band base is 8-byte
-// aligned and the pitch even (then every lane's pair is aligned: its band
-// column is even).
-struct BandOut {
-    float *p;
-    long long pitch;
-    bool vec;
-    __device__ __forceinline__ void init(float *base, long long pit, int q, int row0)
-    {
-        vec = ((reinterpret_cast<uintptr_t>(base) & 7) == 0) && ((pit & 1) == 0);
-        pitch = pit;
-        p = base + q + row0 * pit;
-    }
-    __device__ __forceinline__ void put(float a, float b, bool va, bool vb) const
-    {
-        if (vec && va && vb) {
-            *reinterpret_cast<float2 *>(p) = make_float2(a, b);
-        } else {
-            if (va) p[0] = a;
-            if (vb) p[1] = b;
-        }
-    }
-    __device__ __forceinline__ void advance() { p += pitch; }
-};
-
-// ------------------------------------------------------------ forward, rows
-
-// A unit of single rows: the rows of a one-row image (then the column step
-// only scales by n1), or independent 1D signals stored as rows (rows_only).
-template <int NS>
-__device__ bool forward_rows_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                                  uint64_t *bars, uint32_t &tick, int lane, int *err)
-{
-    const int w = D.w;
-    const int b = strip * kStripOut - 4;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, D.h);
-    const int total = k1 - k0;
-    const int w4 = (w + 3) & ~3;
-    const int lo = max(b, 0), hi = min(b + kStripIn, w4);
-    const uint32_t bytes = uint32_t(hi - lo) * 4u;
-    const int dst_off = lo - b;
-    int off[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) off[i] = min(max(mirror(b + 4 * lane + i, w) - b, lo - b), hi - b - 1);
-    const float *srow = D.in[0] + lo;
-    const long long pitch = D.in_pitch[0];
-    const float scale = D.rows_only ? 1.0f : W.n1_fwd;
-
-    Cursor pc = cursor_at(tick);
-    if (lane == 0) {
-        fence_proxy_async_smem();
-        for (int t = 0; t < min(total, kStages); ++t) {
-            mbar_arrive_expect_tx(&bars[pc.st], bytes);
-            bulk_g2s(ring + pc.st * kStageFloats + dst_off, srow + (long long)(k0 + t) * pitch, bytes,
-                     &bars[pc.st]);
-            pc.next();
-        }
-    }
-    __syncwarp();
-    const int c0 = b + 4 * lane;
-    const bool lane_ok = lane >= 1 && lane <= kLanes - 2;
-    const bool vL0 = lane_ok && c0 < w, vH0 = lane_ok && c0 + 1 < w;
-    const bool vL1 = lane_ok && c0 + 2 < w, vH1 = lane_ok && c0 + 3 < w;
-    const int q = (b >> 1) + 2 * lane;
-    BandOut oL, oH;
-    oL.init(D.out[0], D.out_pitch[0], q, k0);
-    oH.init(D.out[1], D.out_pitch[1], q, k0);
-
-    Cursor c = cursor_at(tick);
-#pragma unroll 1
-    for (int t = 0; t < total; ++t) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
-            if (lane == 0) raise_error(err, kErrWaitTimeout);
-            return false;
-        }
-        const float *slot = ring + c.st * kStageFloats;
-        float A[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) A[i] = slot[off[i]];
-        if (w == 1) {
-            A[0] = fmul(A[0], W.n1_fwd);
-        } else {
-            h_forward<NS>(A, W);
-        }
-        __syncwarp();
-        if (lane == 0 && t + kStages < total) {
-            mbar_arrive_expect_tx(&bars[c.st], bytes);
-            bulk_g2s(ring + c.st * kStageFloats + dst_off, srow + (long long)(k0 + t + kStages) * pitch,
-                     bytes, &bars[c.st]);
-        }
-        c.next();
-        if (!D.rows_only) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) A[i] = fmul(A[i], scale);
-        }
-        oL.put(A[0], A[2], vL0, vL1);
-        oH.put(A[1], A[3], vH0, vH1);
-        oL.advance();
-        oH.advance();
-    }
-    tick += total;
-    return true;
-}
-
-// --------------------------------------------------------------- forward, 2D
-
-// Horizontal forward lifting of one row held as E = (v0, v2) and O = (v1, v3)
-// (the lane's even and odd columns), packed two-wide.
-template <int NS>
-__device__ __forceinline__ void h_forward2(f2 &E, f2 &O, const f2 *C, f2 ZE, f2 ZO)
-{
-#pragma unroll
-    for (int s = 0; s < NS; s += 2) {
-        const float nx = __shfl_down_sync(kFull, f2lo(E), 1);  // next lane's v0
-        O = lift2(O, C[s], E, pk(f2hi(E), nx));                // (v1,v3) += c((v0,v2) + (v2,nx))
-        const float pv = __shfl_up_sync(kFull, f2hi(O), 1);    // previous lane's v3
-        E = lift2(E, C[s + 1], pk(pv, f2lo(O)), O);            // (v0,v2) += c((pv,v1) + (v1,v3))
-    }
-    E = mul2(E, ZE);
-    O = mul2(O, ZO);
-}
-
-template <int NS>
-__device__ __forceinline__ void h_inverse2(f2 &E, f2 &O, const f2 *C, f2 ZE, f2 ZO)
-{
-    E = mul2(E, ZO);
-    O = mul2(O, ZE);
-#pragma unroll
-    for (int s = 0; s < NS; s += 2) {
-        const float pv = __shfl_up_sync(kFull, f2hi(O), 1);
-        E = lift2(E, C[s], pk(pv, f2lo(O)), O);
-        const float nx = __shfl_down_sync(kFull, f2lo(E), 1);
-        O = lift2(O, C[s + 1], E, pk(f2hi(E), nx));
-    }
-}
-
-// Vertical forward recurrence of one packed column pair (see forward_unit).
-template <int NS>
-__device__ __forceinline__ void v_forward2(f2 A, f2 B, f2 &e, f2 &o, f2 &o1, f2 &e1, f2 &o2, const f2 *C,
-                                           f2 ZE, f2 ZO, f2 &L, f2 &H)
-{
-    if (NS == 4) {
-        const f2 o1n = lift2(o, C[0], e, A);    // o'(m-1)
-        const f2 e1n = lift2(e, C[1], o1, o1n); // e'(m-1)
-        const f2 o2n = lift2(o1, C[2], e1, e1n); // o''(m-2)
-        const f2 e2n = lift2(e1, C[3], o2, o2n); // e''(m-2)
-        L = mul2(e2n, ZE);
-        H = mul2(o2n, ZO);
-        o1 = o1n; e1 = e1n; o2 = o2n;
-    } else {
-        const f2 o1n = lift2(o, C[0], e, A);    // o'(m-1)
-        const f2 e1n = lift2(e, C[1], o1, o1n); // e'(m-1)
-        L = mul2(e1n, ZE);
-        H = mul2(o1n, ZO);
-        o1 = o1n;
-    }
-    e = A;
-    o = B;
-}
-
-// One unit of the fused forward level: interleaved rows in, four bands out.
-// Per row pair m (rows 2m, 2m+1, mirrored at the borders) the vertical
-// recurrence emits output pair m - LAT; pairs k0-LAT .. k1+LAT-1 are walked
-// so that the unit's outputs k0 .. k1-1 are exact.  EDGE selects the general
-// path for strips touching the left or right border (mirrored columns,
-// partial lanes) or unaligned outputs.
-template <int NS, bool EDGE>
-__device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                             uint64_t *bars, uint32_t &tick, int lane, int *err)
-{
-    constexpr int LAT = NS / 2;
-    const int w = D.w, h = D.h;
-    const int b = strip * kStripOut - 4;  // interleaved column held by lane 0, value 0
-    const int npairs = (h + 1) >> 1;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, npairs);
-    const int m0 = k0 - LAT;
-    const int total = k1 - k0 + 2 * LAT;  // row pairs walked
-    const int iters = (total + 1) >> 1;   // two pairs per stage
-
-    // staged column window [lo, hi) of every row
-    const int w4 = (w + 3) & ~3;
-    const int lo = max(b, 0), hi = min(b + kStripIn, w4);
-    const uint32_t bytes = uint32_t(hi - lo) * 4u;
-    const int dst_off = lo - b;
-    const float *srow = D.in[0] + lo;
-    const long long pitch = D.in_pitch[0];
-
-    // this lane's shared-memory offsets (mirrored at the borders)
-    int off[4];
-    if (EDGE) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) off[i] = min(max(mirror(b + 4 * lane + i, w) - b, lo - b), hi - b - 1);
-    } else {
-        off[0] = 4 * lane;
-    }
-
-    if (lane == 0) {
-        fence_proxy_async_smem();
-        Cursor pc = cursor_at(tick);
-        const int n0 = min(iters, kStages);
-        for (int u = 0; u < n0; ++u) {
-            float *slot = ring + pc.st * kStageFloats + dst_off;
-            mbar_arrive_expect_tx(&bars[pc.st], 4 * bytes);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * u + r, h, ra, rb);
-                bulk_g2s(slot + (2 * r) * kSlotF, srow + ra * pitch, bytes, &bars[pc.st]);
-                bulk_g2s(slot + (2 * r + 1) * kSlotF, srow + rb * pitch, bytes, &bars[pc.st]);
-            }
-            pc.next();
-        }
-    }
-    __syncwarp();
-
-    // packed constants
-    f2 C[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = pk(W.c[k], W.c[k]);
-    const f2 ZE = pk(W.zeta_e, W.zeta_e), ZO = pk(W.zeta_o, W.zeta_o);
-    const f2 N1 = pk(W.n1_fwd, W.n1_fwd);
-
-    // output geometry of this lane: band column q, stores of (even, odd) pairs
-    const int c0 = b + 4 * lane;
-    const bool lane_ok = lane >= 1 && lane <= kLanes - 2;
-    const bool vL0 = lane_ok && c0 < w, vH0 = lane_ok && c0 + 1 < w;
-    const bool vL1 = lane_ok && c0 + 2 < w, vH1 = lane_ok && c0 + 3 < w;
-    const int q = (b >> 1) + 2 * lane;
-    float *pLL = D.out[0] + q + (long long)k0 * D.out_pitch[0];
-    float *pHL = D.out[1] + q + (long long)k0 * D.out_pitch[1];
-    float *pLH = D.out[2] + q + (long long)k0 * D.out_pitch[2];
-    float *pHH = D.out[3] + q + (long long)k0 * D.out_pitch[3];
-    const int last_h = (h >> 1) - 1;  // last output pair with an H row
-
-    f2 e[2] = {0, 0}, o[2] = {0, 0}, o1[2] = {0, 0}, e1[2] = {0, 0}, o2[2] = {0, 0};
-
-    Cursor c = cursor_at(tick);
-    int t = 0;  // pair counter
-#pragma unroll 1
-    for (int u = 0; u < iters; ++u) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
-            if (lane == 0) raise_error(err, kErrWaitTimeout);
-            return false;
-        }
-        const float *slot = ring + c.st * kStageFloats;
-        f2 E[4], O[4];  // rows 0..3 of the stage
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const float *row = slot + r * kSlotF;
-            if (EDGE) {
-                E[r] = pk(row[off[0]], row[off[2]]);
-                O[r] = pk(row[off[1]], row[off[3]]);
-            } else {
-                const float4 v = *reinterpret_cast<const float4 *>(row + off[0]);
-                E[r] = pk(v.x, v.z);
-                O[r] = pk(v.y, v.w);
-            }
-        }
-        // rows: horizontal lifting (a single-sample row is only scaled)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            if (w == 1) {
-                E[r] = mul2(E[r], N1);
-            } else {
-                h_forward2<NS>(E[r], O[r], C, ZE, ZO);
-            }
-        }
-        // the stage is consumed: refill it with the pairs kStages stages ahead
-        __syncwarp();
-        if (lane == 0 && u + kStages < iters) {
-            float *dst = ring + c.st * kStageFloats + dst_off;
-            mbar_arrive_expect_tx(&bars[c.st], 4 * bytes);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * (u + kStages) + r, h, ra, rb);
-                bulk_g2s(dst + (2 * r) * kSlotF, srow + ra * pitch, bytes, &bars[c.st]);
-                bulk_g2s(dst + (2 * r + 1) * kSlotF, srow + rb * pitch, bytes, &bars[c.st]);
-            }
-        }
-        c.next();
-
-        // columns: two steps of the vertical recurrence (two row pairs)
-#pragma unroll
-        for (int r = 0; r < 2; ++r, ++t) {
-            f2 LE, HE, LO, HO;
-            v_forward2<NS>(E[2 * r], E[2 * r + 1], e[0], o[0], o1[0], e1[0], o2[0], C, ZE, ZO, LE, HE);
-            v_forward2<NS>(O[2 * r], O[2 * r + 1], e[1], o[1], o1[1], e1[1], o2[1], C, ZE, ZO, LO, HO);
-            if (t >= 2 * LAT && t < total) {
-                const int p = m0 + t - LAT;
-                if (EDGE) {
-                    if (vL0) pLL[0] = f2lo(LE);
-                    if (vL1) pLL[1] = f2hi(LE);
-                    if (vH0) pHL[0] = f2lo(LO);
-                    if (vH1) pHL[1] = f2hi(LO);
-                    if (p <= last_h) {
-                        if (vL0) pLH[0] = f2lo(HE);
-                        if (vL1) pLH[1] = f2hi(HE);
-                        if (vH0) pHH[0] = f2lo(HO);
-                        if (vH1) pHH[1] = f2hi(HO);
-                    }
-                } else if (lane_ok) {
-                    *reinterpret_cast<f2 *>(pLL) = LE;
-                    *reinterpret_cast<f2 *>(pHL) = LO;
-                    if (p <= last_h) {
-                        *reinterpret_cast<f2 *>(pLH) = HE;
-                        *reinterpret_cast<f2 *>(pHH) = HO;
-                    }
-                }
-                pLL += D.out_pitch[0];
-                pHL += D.out_pitch[1];
-                pLH += D.out_pitch[2];
-                pHH += D.out_pitch[3];
-            }
-        }
-    }
-    tick += iters;
-    return true;
-}
-
-// ------------------------------------------------------------------ inverse
-
-// One band's staged window: its row 0 start rounded down to 16 bytes, the
-// byte count per row and the float shift of the wanted first column.
-struct BandIn {
-    const float *base;  // 16-byte aligned start in row 0
-    long long pitch;
-    uint32_t bytes;
-    int shift;
-    __device__ __forceinline__ void init(const float *band, long long pit, int lo, int n)
-    {
-        pitch = pit;
-        if (n <= 0) {
-            bytes = 0;
-            shift = 0;
-            base = band;
-            return;
-        }
-        const uintptr_t a = reinterpret_cast<uintptr_t>(band + lo);
-        const uintptr_t a0 = a & ~uintptr_t(15);
-        const uintptr_t e = (a + uintptr_t(n) * 4 + 15) & ~uintptr_t(15);
-        base = reinterpret_cast<const float *>(a0);
-        bytes = uint32_t(e - a0);
-        shift = int((a - a0) >> 2);
-    }
-};
-
-// Inverse units of single rows (one-row images and rows_only signals).
-template <int NS>
-__device__ bool inverse_rows_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                                  uint64_t *bars, uint32_t &tick, int lane, int *err)
-{
-    const int w = D.w;
-    const int b = strip * kStripOut - 4;
-    const int bq = b >> 1;
-    const int Lw = (w + 1) >> 1, Hw = w >> 1;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, D.h);
-    const int total = k1 - k0;
-    const int loL = max(bq, 0), hiL = min(bq + 64, Lw);
-    const int loH = loL, hiH = min(bq + 64, Hw);
-    BandIn iL, iH;
-    iL.init(D.in[0], D.in_pitch[0], loL, hiL - loL);
-    iH.init(D.in[1], D.in_pitch[1], loH, hiH - loH);
-    int off[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        int bi = 0, k = 0;
-        if (w != 1) {
-            const int mc = mirror(b + 4 * lane + i, w);
-            bi = mc >> 1;
-            k = mc & 1;
-        }
-        const int o = bi - (k ? loH : loL) + (k ? iH.shift : iL.shift);
-        off[i] = k * kSlotI + min(max(o, 0), kSlotI - 1);
-    }
-    const uint32_t tx = iL.bytes + iH.bytes;
-    auto issue = [&](int row, const Cursor &pc) {
-        float *slot = ring + pc.st * kStageFloats;
-        mbar_arrive_expect_tx(&bars[pc.st], tx);
-        bulk_g2s(slot, iL.base + row * iL.pitch, iL.bytes, &bars[pc.st]);
-        if (iH.bytes) bulk_g2s(slot + kSlotI, iH.base + row * iH.pitch, iH.bytes, &bars[pc.st]);
-    };
-    if (lane == 0) {
-        fence_proxy_async_smem();
-        Cursor pc = cursor_at(tick);
-        for (int t = 0; t < min(total, kStages); ++t) {
-            issue(k0 + t, pc);
-            pc.next();
-        }
-    }
-    __syncwarp();
-    const int c0 = b + 4 * lane;
-    const bool lane_ok = lane >= 1 && lane <= kLanes - 2;
-    bool ok[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) ok[i] = lane_ok && (c0 + i < w);
-    const float scale = D.rows_only ? 1.0f : W.n1_inv;
-    float *orow = D.out[0] + c0 + (long long)k0 * D.out_pitch[0];
-
-    Cursor c = cursor_at(tick);
-#pragma unroll 1
-    for (int t = 0; t < total; ++t) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
-            if (lane == 0) raise_error(err, kErrWaitTimeout);
-            return false;
-        }
-        const float *slot = ring + c.st * kStageFloats;
-        float A[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) A[i] = slot[off[i]];
-        if (w == 1) {
-            A[0] = fmul(A[0], W.n1_inv);
-        } else {
-            h_inverse<NS>(A, W);
-        }
-        __syncwarp();
-        if (lane == 0 && t + kStages < total) issue(k0 + t + kStages, c);
-        c.next();
-        if (!D.rows_only) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) A[i] = fmul(A[i], scale);
-        }
-        store4(orow, A, ok);
-        orow += D.out_pitch[0];
-    }
-    tick += total;
-    return true;
-}
-
-// Vertical inverse recurrence of one packed column pair (see inverse_unit).
-template <int NS>
-__device__ __forceinline__ void v_inverse2(f2 A, f2 B, f2 &o, f2 &e1, f2 &o1, f2 &e2, const f2 *C, f2 ZE,
-                                           f2 ZO, f2 &Ev, f2 &Ov)
-{
-    const f2 E = mul2(A, ZO);  // pre-scale: even x (1/zeta)
-    const f2 O = mul2(B, ZE);  //            odd  x zeta
-    if (NS == 4) {
-        const f2 e1n = lift2(E, C[0], o, O);      // e'(m)
-        const f2 o1n = lift2(o, C[1], e1, e1n);   // o'(m-1)
-        const f2 e2n = lift2(e1, C[2], o1, o1n);  // e''(m-1)
-        const f2 o2n = lift2(o1, C[3], e2, e2n);  // o''(m-2)
-        Ev = e2;                                  // e''(m-2)
-        Ov = o2n;
-        e1 = e1n; o1 = o1n; e2 = e2n;
-    } else {
-        const f2 e1n = lift2(E, C[0], o, O);      // e'(m)
-        const f2 o1n = lift2(o, C[1], e1, e1n);   // o'(m-1)
-        Ev = e1;                                  // e'(m-1)
-        Ov = o1n;
-        e1 = e1n;
-    }
-    o = O;
-}
-
-// One unit of the fused inverse level: four bands in, interleaved rows out.
-// Per pair m the stage holds the LL and HL rows of L-row ra/2 and the LH and
-// HH rows of H-row rb/2 (ra, rb the mirrored interleaved rows 2m, 2m+1); the
-// horizontal inverse rebuilds both interleaved rows, the vertical recurrence
-// emits output rows 2(m-LAT), 2(m-LAT)+1.
-template <int NS, bool EDGE>
-__device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                             uint64_t *bars, uint32_t &tick, int lane, int *err)
-{
-    constexpr int LAT = NS / 2;
-    const int w = D.w, h = D.h;
-    const int b = strip * kStripOut - 4;
-    const int bq = b >> 1;  // band column of lane 0's first value
-    const int Lw = (w + 1) >> 1, Hw = w >> 1;
-    const int npairs = (h + 1) >> 1;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, npairs);
-    const int m0 = k0 - LAT;
-    const int total = k1 - k0 + 2 * LAT;
-    const int iters = (total + 1) >> 1;
-
-    // staged band column windows; the shift is the same for every row
-    // because source pitches are multiples of 4 floats
-    const int loL = max(bq, 0), hiL = min(bq + 64, Lw);
-    const int loH = loL, hiH = min(bq + 64, Hw);
-    BandIn iLL, iHL, iLH, iHH;
-    iLL.init(D.in[0], D.in_pitch[0], loL, hiL - loL);
-    iHL.init(D.in[1], D.in_pitch[1], loH, hiH - loH);
-    iLH.init(D.in[2], D.in_pitch[2], loL, hiL - loL);
-    iHH.init(D.in[3], D.in_pitch[3], loH, hiH - loH);
-    const uint32_t tx = 2 * (iLL.bytes + iHL.bytes + iLH.bytes + iHH.bytes);
-
-    // this lane's offsets inside a pair's 4 band-row slots: even samples from
-    // the L bands (slots 0, 2), odd samples from the H bands (slots 1, 3)
-    int offA[4], offB[4];
-    if (EDGE) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            int bi = 0, k = 0;
-            if (w != 1) {
-                const int mc = mirror(b + 4 * lane + i, w);
-                bi = mc >> 1;
-                k = mc & 1;
-            }
-            const int lo_k = k ? loH : loL;
-            const int oa = bi - lo_k + (k ? iHL.shift : iLL.shift);
-            const int ob = bi - lo_k + (k ? iHH.shift : iLH.shift);
-            offA[i] = k * kSlotI + min(max(oa, 0), kSlotI - 1);
-            offB[i] = (2 + k) * kSlotI + min(max(ob, 0), kSlotI - 1);
-        }
-    } else {
-        offA[0] = 2 * lane + iLL.shift;
-        offA[1] = kSlotI + 2 * lane + iHL.shift;
-        offB[0] = 2 * kSlotI + 2 * lane + iLH.shift;
-        offB[1] = 3 * kSlotI + 2 * lane + iHH.shift;
-    }
-
-    if (lane == 0) {
-        fence_proxy_async_smem();
-        Cursor pc = cursor_at(tick);
-        const int n0 = min(iters, kStages);
-        for (int u = 0; u < n0; ++u) {
-            float *slot = ring + pc.st * kStageFloats;
-            mbar_arrive_expect_tx(&bars[pc.st], tx);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * u + r, h, ra, rb);
-                const int qa = ra >> 1, qb = rb >> 1;
-                float *sl = slot + 4 * r * kSlotI;
-                bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, &bars[pc.st]);
-                bulk_g2s(sl + 2 * kSlotI, iLH.base + qb * iLH.pitch, iLH.bytes, &bars[pc.st]);
-                if (iHL.bytes) {
-                    bulk_g2s(sl + kSlotI, iHL.base + qa * iHL.pitch, iHL.bytes, &bars[pc.st]);
-                    bulk_g2s(sl + 3 * kSlotI, iHH.base + qb * iHH.pitch, iHH.bytes, &bars[pc.st]);
-                }
-            }
-            pc.next();
-        }
-    }
-    __syncwarp();
-
-    f2 C[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = pk(W.c[k], W.c[k]);
-    const f2 ZE = pk(W.zeta_e, W.zeta_e), ZO = pk(W.zeta_o, W.zeta_o);
-    const f2 N1 = pk(W.n1_inv, W.n1_inv);
-
-    const int c0 = b + 4 * lane;
-    const bool lane_ok = lane >= 1 && lane <= kLanes - 2;
-    bool ok[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) ok[i] = lane_ok && (c0 + i < w);
-    const long long opitch = D.out_pitch[0];
-    float *orow = D.out[0] + c0 + (long long)(2 * k0) * opitch;  // row 2p of output pair p
-    const int last_odd = (h >> 1) - 1;
-
-    f2 o[2] = {0, 0}, e1[2] = {0, 0}, o1[2] = {0, 0}, e2[2] = {0, 0};
-
-    Cursor c = cursor_at(tick);
-    int t = 0;
-#pragma unroll 1
-    for (int u = 0; u < iters; ++u) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
-            if (lane == 0) raise_error(err, kErrWaitTimeout);
-            return false;
-        }
-        const float *slot = ring + c.st * kStageFloats;
-        f2 E[4], O[4];  // interleaved rows: pair 0 L-row, H-row, pair 1 L-row, H-row
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float *sl = slot + 4 * r * kSlotI;
-            if (EDGE) {
-                E[2 * r] = pk(sl[offA[0]], sl[offA[2]]);
-                O[2 * r] = pk(sl[offA[1]], sl[offA[3]]);
-                E[2 * r + 1] = pk(sl[offB[0]], sl[offB[2]]);
-                O[2 * r + 1] = pk(sl[offB[1]], sl[offB[3]]);
-            } else {
-                E[2 * r] = *reinterpret_cast<const f2 *>(sl + offA[0]);
-                O[2 * r] = *reinterpret_cast<const f2 *>(sl + offA[1]);
-                E[2 * r + 1] = *reinterpret_cast<const f2 *>(sl + offB[0]);
-                O[2 * r + 1] = *reinterpret_cast<const f2 *>(sl + offB[1]);
-            }
-        }
-        // rows first (src/libdwt.c:6706-6717), then columns
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            if (w == 1) {
-                E[r] = mul2(E[r], N1);
-            } else {
-                h_inverse2<NS>(E[r], O[r], C, ZE, ZO);
-            }
-        }
-        __syncwarp();
-        if (lane == 0 && u + kStages < iters) {
-            float *slot2 = ring + c.st * kStageFloats;
-            mbar_arrive_expect_tx(&bars[c.st], tx);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * (u + kStages) + r, h, ra, rb);
-                const int qa = ra >> 1, qb = rb >> 1;
-                float *sl = slot2 + 4 * r * kSlotI;
-                bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, &bars[c.st]);
-                bulk_g2s(sl + 2 * kSlotI, iLH.base + qb * iLH.pitch, iLH.bytes, &bars[c.st]);
-                if (iHL.bytes) {
-                    bulk_g2s(sl + kSlotI, iHL.base + qa * iHL.pitch, iHL.bytes, &bars[c.st]);
-                    bulk_g2s(sl + 3 * kSlotI, iHH.base + qb * iHH.pitch, iHH.bytes, &bars[c.st]);
-                }
-            }
-        }
-        c.next();
-
-#pragma unroll
-        for (int r = 0; r < 2; ++r, ++t) {
-            f2 EvE, OvE, EvO, OvO;
-            v_inverse2<NS>(E[2 * r], E[2 * r + 1], o[0], e1[0], o1[0], e2[0], C, ZE, ZO, EvE, OvE);
-            v_inverse2<NS>(O[2 * r], O[2 * r + 1], o[1], e1[1], o1[1], e2[1], C, ZE, ZO, EvO, OvO);
-            if (t >= 2 * LAT && t < total) {
-                const int p = m0 + t - LAT;
-                if (EDGE) {
-                    const float ev[4] = {f2lo(EvE), f2lo(EvO), f2hi(EvE), f2hi(EvO)};
-                    store4(orow, ev, ok);
-                    if (p <= last_odd) {
-                        const float ov[4] = {f2lo(OvE), f2lo(OvO), f2hi(OvE), f2hi(OvO)};
-                        store4(orow + opitch, ov, ok);
-                    }
-                } else if (lane_ok) {
-                    *reinterpret_cast<float4 *>(orow) = make_float4(f2lo(EvE), f2lo(EvO), f2hi(EvE), f2hi(EvO));
-                    if (p <= last_odd)
-                        *reinterpret_cast<float4 *>(orow + opitch) =
-                            make_float4(f2lo(OvE), f2lo(OvO), f2hi(OvE), f2hi(OvO));
-                }
-                orow += 2 * opitch;
-            }
-        }
-    }
-    tick += iters;
-    return true;
-}
 
 template <int NS, bool INV>
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
@@ -796,51 +27,15 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float *ring = reinterpret_cast<float *>(smem) + warp * kStages * kStageFloats;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kWarpsPerCta * kStages * kStageFloats * 4) +
-                     warp * kStages;
-    if (lane == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
-        fence_mbar_init();
-    }
-    __syncwarp();
-
-    // interior units may use vector loads and stores when every band pointer
-    // and pitch keeps them aligned
-    bool fast_launch;
-    if (INV) {
-        fast_launch = ((reinterpret_cast<uintptr_t>(D.out[0]) & 15) == 0) && ((D.out_pitch[0] & 3) == 0);
-        for (int k = 0; k < 4; ++k) {
-            // LDS.64 of band pairs needs an even float shift of every band row
-            const uintptr_t a = reinterpret_cast<uintptr_t>(D.in[k]);
-            fast_launch = fast_launch && ((a & 7) == 0) && ((D.in_pitch[k] & 3) == 0);
-        }
-    } else {
-        fast_launch = true;
-        for (int k = 0; k < 4; ++k)
-            fast_launch = fast_launch && ((reinterpret_cast<uintptr_t>(D.out[k]) & 7) == 0) &&
-                          ((D.out_pitch[k] & 1) == 0);
-    }
-
+    float *ring = units::warp_ring(smem, warp);
+    uint64_t *bars = units::warp_bars(smem, warp, kWarpsPerCta);
+    units::init_bars(bars, lane);
+    const bool fast_launch = units::fast_ok<INV>(D);
     uint32_t tick = 0;
-    const int units = D.n_strips * D.n_segs;
-    for (int u = blockIdx.x * kWarpsPerCta + warp; u < units; u += gridDim.x * kWarpsPerCta) {
+    const int n = D.n_strips * D.n_segs;
+    for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
         const int strip = u % D.n_strips, seg = u / D.n_strips;
-        bool ok;
-        if (D.h == 1 || D.rows_only) {
-            ok = INV ? inverse_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err)
-                     : forward_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err);
-        } else {
-            const int b = strip * kStripOut - 4;
-            const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
-            if (INV)
-                ok = edge ? inverse_unit<NS, true>(D, W, strip, seg, ring, bars, tick, lane, err)
-                          : inverse_unit<NS, false>(D, W, strip, seg, ring, bars, tick, lane, err);
-            else
-                ok = edge ? forward_unit<NS, true>(D, W, strip, seg, ring, bars, tick, lane, err)
-                          : forward_unit<NS, false>(D, W, strip, seg, ring, bars, tick, lane, err);
-        }
-        if (!ok) break;
+        if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch)) break;
     }
 }
 

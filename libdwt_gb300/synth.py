@@ -51,3 +51,34 @@ def ar1_bank(groups: int, n: int, lanes: int, seed: int = 0, rho: float = 0.95) 
         prev = prev * np.float32(rho) + eps[:, i, :]
         x[:, i, :] = prev
     return x
+
+
+def image_torch(w: int, h: int, seed: int = 0, blobs: int = 64, device: str = "cuda"):
+    """The recipe of image() on the GPU with torch (same distribution; values
+    are not bit-identical to the numpy version)."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    cx = torch.rand(blobs, generator=g, dtype=torch.float64) * w
+    cy = torch.rand(blobs, generator=g, dtype=torch.float64) * h
+    sig = 8 + torch.rand(blobs, generator=g, dtype=torch.float64) * 120
+    amp = torch.rand(blobs, generator=g, dtype=torch.float64) * 2 - 1
+    xs = torch.arange(w, dtype=torch.float64)
+    ys = torch.arange(h, dtype=torch.float64)
+    gx = torch.exp(-((xs[None, :] - cx[:, None]) ** 2) / (2 * sig[:, None] ** 2)).float().to(device)
+    gy = (torch.exp(-((ys[:, None] - cy[None, :]) ** 2) / (2 * sig[None, :] ** 2)) * amp[None, :]).float().to(device)
+    field = gy @ gx
+    lo, hi = field.min(), field.max()
+    field = (field - lo) * (255.0 / torch.clamp(hi - lo, min=1e-20))
+    gn = torch.Generator(device=device).manual_seed(seed + 1)
+    field += torch.randn(field.shape, generator=gn, device=device) * 2.0
+    return torch.round(torch.clamp(field, 0, 255))
+
+
+def batch_sizes(n: int, lo: int = 33, hi: int = 2048, seed: int = 0):
+    """n (w, h) pairs, each side log-uniform in [lo, hi], and a wavelet per
+    image (0 = CDF 9/7, 1 = CDF 5/3, 50/50)."""
+    rng = np.random.default_rng(seed)
+    w = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n))).astype(int)
+    h = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n))).astype(int)
+    wav = rng.integers(0, 2, n)
+    return list(zip(w.tolist(), h.tolist(), wav.tolist()))
