@@ -220,11 +220,14 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--level-reps", type=int, default=50)
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the serving replay in the extras")
     ap.add_argument("--image", type=int, default=16384,
                     help="image side (a smaller case for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    global W, H, J, WORKLOAD
+    global W, H, J, WORKLOAD, SERVE_SECONDS
+    SERVE_SECONDS = args.serve_seconds
     if args.image != 16384:
         W = H = args.image
         J = int(np.ceil(np.log2(W)))
@@ -433,7 +436,58 @@ def run_extras(D, torch, stream, sptr):
         c0dev()
     out["c0_1024_fwd_inv_device_ms"] = round((time.perf_counter() - t) / n * 1e3, 3)
     out.update(run_batch_extra(D, torch, stream, sptr))
+    out.update(run_serve_extra(D, torch, SERVE_SECONDS))
     return out
+
+
+SERVE_SECONDS = 10.0
+
+
+def serve_trace(seconds: float, rate: float = 20000.0, seed: int = 11):
+    """Poisson arrivals (mean `rate` per second) of forward or inverse 2D
+    transforms: area log-uniform in 32^2..8192^2, aspect ratio uniform in
+    [0.5, 2], CDF 9/7 or 5/3 and direction 50/50, j_max uniform in 1..6."""
+    rng = np.random.default_rng(seed)
+    n = int(rate * seconds * 1.1) + 16
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    t = t[t < seconds]
+    n = len(t)
+    area = np.exp(rng.uniform(np.log(32 * 32), np.log(8192 * 8192), n))
+    a = rng.uniform(0.5, 2.0, n)
+    w = np.maximum(1, np.rint(np.sqrt(area * a))).astype(int)
+    h = np.maximum(1, np.rint(np.sqrt(area / a))).astype(int)
+    wav = rng.integers(0, 2, n)
+    inv = rng.integers(0, 2, n)
+    j = rng.integers(1, 7, n)
+    return t, w, h, wav, inv, j
+
+
+def run_serve_extra(D, torch, seconds: float):
+    """Serving loop: a 20k req/s Poisson stream replayed in real time against
+    the continuous-batching server (64 GiB admission budget, pooled buffers);
+    every request reads its w x h input from a resident synthetic image and
+    writes its result to a pooled buffer."""
+    from libdwt_gb300 import synth
+    t, w, h, wav, inv, j = serve_trace(seconds)
+    side = int(max(w.max(), h.max()))
+    pitch = (side + 3) // 4 * 4
+    src = torch.empty((side, pitch), dtype=torch.float32, device="cuda")
+    src[:, :side] = synth.image_torch(side, side, seed=5)
+    torch.cuda.synchronize()
+    reqs = [D.Server.request(src, None, "cdf97" if wav[k] == 0 else "cdf53", bool(inv[k]), int(j[k]), tag=k,
+                             w=int(w[k]), h=int(h[k])) for k in range(len(t))]
+    srv = D.Server(budget_bytes=64 << 30, n_streams=4)
+    t0 = time.perf_counter()
+    lat = srv.replay(t, reqs, timeout_s=600)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    px = float((w.astype(np.int64) * h).sum())
+    return {"c3_seconds": seconds, "c3_requests": int(len(t)), "c3_offered_mpx_s": round(px / seconds / 1e6, 1),
+            "c3_sustained_mpx_s": round(px / wall / 1e6, 1), "c3_p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+            "c3_p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+            "c3_max_ms": round(float(lat.max()) * 1e3, 3), "c3_launches": st["launches"],
+            "c3_peak_bytes": st["peak_bytes"], "c3_budget_bytes": st["budget_bytes"]}
 
 
 def run_batch_extra(D, torch, stream, sptr, n_images=4096, j=4):

@@ -224,6 +224,61 @@ DWT_EXPORT int dwt_gpu_batch_params_get(const dwt_gpu_batch *b, dwt_gpu_batch_pa
 DWT_EXPORT int dwt_gpu_batch_items(const dwt_gpu_batch *b);
 DWT_EXPORT void dwt_gpu_batch_destroy(dwt_gpu_batch *b);
 
+/* --------------------------------------------------------------- serving */
+
+/* One transform request: src a device frame (rows 16-byte aligned), dst a
+ * device frame or NULL (the server then writes into a pooled buffer it
+ * releases on completion), w x h, j_levels < 0 for the full depth. */
+typedef struct {
+    const float *src;
+    long long src_pitch_bytes;
+    float *dst;
+    long long dst_pitch_bytes;
+    int w, h;
+    int j_levels;
+    int decompose_one;
+    int wavelet;
+    int inverse;
+    long long tag; /* returned with the completion */
+} dwt_gpu_request;
+
+/* A finished request; times in seconds on the steady clock. */
+typedef struct {
+    long long id;
+    long long tag;
+    int status;
+    double t_submit;
+    double t_admit;
+    double t_complete;
+} dwt_gpu_completion;
+
+typedef struct {
+    long long submitted, completed, launches, pending;
+    long long bytes_in_use, peak_bytes, budget_bytes;
+} dwt_gpu_server_stats_t;
+
+typedef struct dwt_gpu_server dwt_gpu_server;
+
+/* Starts a server: requests are admitted in arrival order while their device
+ * memory (scratch + pooled output) fits `budget_bytes`, grouped into
+ * micro-batches of the batched kernel and run on `n_streams` streams that
+ * overlap on the device.  params = NULL uses (32, 32, 4). */
+DWT_EXPORT int dwt_gpu_server_create(dwt_gpu_server **out, long long budget_bytes, int n_streams,
+                                     const dwt_gpu_batch_params *params);
+/* Queues a request (never blocks); DWT_GPU_EBUSY if it alone exceeds the budget. */
+DWT_EXPORT int dwt_gpu_server_submit(dwt_gpu_server *s, const dwt_gpu_request *r, long long *id);
+/* Takes up to `max` completions. */
+DWT_EXPORT int dwt_gpu_server_poll(dwt_gpu_server *s, dwt_gpu_completion *out, int max, int *n);
+/* Waits until every submitted request completed (DWT_GPU_EBUSY on timeout). */
+DWT_EXPORT int dwt_gpu_server_drain(dwt_gpu_server *s, double timeout_s);
+DWT_EXPORT int dwt_gpu_server_stats(dwt_gpu_server *s, dwt_gpu_server_stats_t *st);
+/* Submits reqs[i] at arrival_s[i] seconds after the call (real time, from
+ * the calling thread), drains, and writes each request's arrival-to-
+ * completion latency. */
+DWT_EXPORT int dwt_gpu_server_replay(dwt_gpu_server *s, int n, const double *arrival_s,
+                                     const dwt_gpu_request *reqs, double *latency_s, double timeout_s);
+DWT_EXPORT void dwt_gpu_server_destroy(dwt_gpu_server *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,25 @@ class BatchImage(C.Structure):
                 ("inverse", _i)]
 
 
+class Request(C.Structure):
+    """dwt_gpu_request (include/libdwt.h)."""
+    _fields_ = [("src", _vp), ("src_pitch_bytes", _ll), ("dst", _vp), ("dst_pitch_bytes", _ll),
+                ("w", _i), ("h", _i), ("j_levels", _i), ("decompose_one", _i), ("wavelet", _i),
+                ("inverse", _i), ("tag", _ll)]
+
+
+class Completion(C.Structure):
+    """dwt_gpu_completion (include/libdwt.h)."""
+    _fields_ = [("id", _ll), ("tag", _ll), ("status", _i), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_complete", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """dwt_gpu_server_stats_t (include/libdwt.h)."""
+    _fields_ = [("submitted", _ll), ("completed", _ll), ("launches", _ll), ("pending", _ll),
+                ("bytes_in_use", _ll), ("peak_bytes", _ll), ("budget_bytes", _ll)]
+
+
 class BatchParams(C.Structure):
     """dwt_gpu_batch_params (include/libdwt.h)."""
     _fields_ = [("seg_pairs", _i), ("tail_side", _i), ("ctas_per_sm", _i)]
@@ -75,6 +94,14 @@ def lib():
         L.dwt_gpu_batch_items.argtypes = [C.c_void_p]
         L.dwt_gpu_batch_destroy.argtypes = [C.c_void_p]
         L.dwt_gpu_sync_check.restype = _i
+        L.dwt_gpu_server_create.argtypes = [C.POINTER(C.c_void_p), _ll, _i, C.POINTER(BatchParams)]
+        L.dwt_gpu_server_submit.argtypes = [C.c_void_p, C.POINTER(Request), C.POINTER(_ll)]
+        L.dwt_gpu_server_poll.argtypes = [C.c_void_p, C.POINTER(Completion), _i, C.POINTER(_i)]
+        L.dwt_gpu_server_drain.argtypes = [C.c_void_p, C.c_double]
+        L.dwt_gpu_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+        L.dwt_gpu_server_replay.argtypes = [C.c_void_p, _i, C.POINTER(C.c_double), C.POINTER(Request),
+                                            C.POINTER(C.c_double), C.c_double]
+        L.dwt_gpu_server_destroy.argtypes = [C.c_void_p]
         L.dwt_gpu_error_string.restype = C.c_char_p
         L.dwt_gpu_error_string.argtypes = [_i]
         L.dwt_util_set_accel.argtypes = [_i]
@@ -258,6 +285,64 @@ class Batch:
     def close(self) -> None:
         if self._h:
             lib().dwt_gpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The continuous-batching server (dwt_gpu_server_*)."""
+
+    def __init__(self, budget_bytes: int, n_streams: int = 4, params=None):
+        self._h = C.c_void_p()
+        p = None if params is None else C.byref(BatchParams(*params))
+        _check(lib().dwt_gpu_server_create(C.byref(self._h), budget_bytes, n_streams, p))
+
+    @staticmethod
+    def request(src, dst, wavelet, inverse=False, j_levels=-1, tag=0, w=None, h=None) -> Request:
+        """A request on torch CUDA tensors; dst=None lets the server write to a pooled buffer."""
+        hh, ww = (dst.shape if dst is not None else src.shape) if w is None else (h, w)
+        return Request(src.data_ptr() if hasattr(src, "data_ptr") else src,
+                       src.stride(0) * 4 if hasattr(src, "stride") else 0,
+                       None if dst is None else dst.data_ptr(), 0 if dst is None else dst.stride(0) * 4,
+                       ww, hh, j_levels, 0, _WAVELETS[wavelet], 1 if inverse else 0, tag)
+
+    def submit(self, req: Request) -> int:
+        i = _ll()
+        _check(lib().dwt_gpu_server_submit(self._h, C.byref(req), C.byref(i)))
+        return i.value
+
+    def poll(self, max_n: int = 4096):
+        buf = (Completion * max_n)()
+        n = _i()
+        _check(lib().dwt_gpu_server_poll(self._h, buf, max_n, C.byref(n)))
+        return [buf[k] for k in range(n.value)]
+
+    def drain(self, timeout_s: float = 60.0) -> None:
+        _check(lib().dwt_gpu_server_drain(self._h, timeout_s))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().dwt_gpu_server_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def replay(self, arrival_s, reqs, timeout_s: float = 300.0):
+        """Submit reqs[i] at arrival_s[i] (real time), drain; returns latencies (s)."""
+        import numpy as np
+        n = len(reqs)
+        arr = (C.c_double * n)(*[float(a) for a in arrival_s])
+        rq = (Request * n)(*reqs)
+        lat = (C.c_double * n)()
+        _check(lib().dwt_gpu_server_replay(self._h, n, arr, rq, lat, timeout_s))
+        return np.frombuffer(lat, dtype=np.float64).copy()
+
+    def close(self) -> None:
+        if self._h:
+            lib().dwt_gpu_server_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -32,35 +32,12 @@
 #include <vector>
 
 #include "../../include/libdwt.h"
+#include "dwt_batch.cuh"
 #include "dwt_capi_internal.h"
 #include "dwt_lines.cuh"
 #include "dwt_units.cuh"
 
 namespace dwt {
-
-constexpr int kMaxLevels = 16;
-constexpr int kPhases = kMaxLevels + 1;
-constexpr int kBatchWarps = 4;  // warps per CTA (the per-level kernel's shape)
-
-struct BatchImage {
-    const float *src;
-    long long src_pitch;  // floats, rows 16-byte aligned
-    float *dst;
-    long long dst_pitch;  // floats
-    float *ll[2];         // LL scratch frames (ping-pong)
-    long long llp[2];
-    int w, h, J, wavelet, inverse;
-    int j_tail;  // first level run by the tail item (== J: no tail)
-    int seg[kMaxLevels], n_strips[kMaxLevels], n_segs[kMaxLevels];  // per level j (0-based)
-    int units[kPhases];  // items per phase
-};
-
-struct BatchItem {
-    int image;
-    int phase;
-    int level;  // level index j (forward: j -> j+1; inverse: j -> j-1), -1 for the tail
-    int unit;   // strip + seg * n_strips
-};
 
 namespace {
 
@@ -319,69 +296,13 @@ int build_plan(dwt_gpu_batch *b)
     size_t arena_floats = 0;
     b->plain_copy.clear();
     for (int i = 0; i < b->n; ++i) {
-        const dwt_gpu_batch_image &u = b->images[i];
-        BatchImage &I = imgs[i];
-        memset(&I, 0, sizeof(I));
-        const int lim = ceil_log2_int(u.decompose_one ? std::max(u.w, u.h) : std::min(u.w, u.h));
-        const int J = (u.j_levels < 0 || u.j_levels > lim) ? lim : u.j_levels;
-        I.src = u.src;
-        I.src_pitch = u.src_pitch_bytes / 4;
-        I.dst = u.dst;
-        I.dst_pitch = u.dst_pitch_bytes / 4;
-        I.w = u.w;
-        I.h = u.h;
-        I.J = J;
-        I.wavelet = u.wavelet;
-        I.inverse = u.inverse;
-        if (J == 0) {
+        const size_t sf = plan_image(imgs[i], b->images[i], P, i, by_phase);
+        if (imgs[i].J == 0) {
             b->plain_copy.push_back(i);
             continue;
         }
-        long long p0, p1;
-        const size_t sf = dense_scratch_floats(u.w, u.h, J, &p0, &p1);
         scratch_off[i] = arena_floats;
         arena_floats += align_up_ll((long long)sf, 64);
-        I.llp[0] = p0;
-        I.llp[1] = p1;
-        // the first level whose band the tail item takes
-        I.j_tail = J;
-        for (int j = 0; j < J; ++j)
-            if (tail_fits(ceil_div_pow2(u.w, j), ceil_div_pow2(u.h, j), P.tail_side)) {
-                I.j_tail = j;
-                break;
-            }
-        for (int j = 0; j < J; ++j) {
-            const int w = ceil_div_pow2(u.w, j), h = ceil_div_pow2(u.h, j);
-            const int npairs = (h == 1) ? 1 : (h + 1) / 2;
-            I.n_strips[j] = ceil_div(w, kStripOut);
-            I.seg[j] = std::max(1, std::min(P.seg_pairs, npairs));
-            I.n_segs[j] = ceil_div(npairs, I.seg[j]);
-        }
-        // phases and items
-        int phase = 0;
-        auto level_units = [&](int jidx) { return I.n_strips[jidx] * I.n_segs[jidx]; };
-        if (!u.inverse) {
-            for (int j = 0; j < I.j_tail; ++j, ++phase) {
-                I.units[phase] = level_units(j);
-                for (int k = 0; k < I.units[phase]; ++k) by_phase[phase].push_back({i, phase, j, k});
-            }
-            if (I.j_tail < J) {
-                I.units[phase] = 1;
-                by_phase[phase].push_back({i, phase, -1, 0});
-            }
-        } else {
-            int jtop = J;
-            if (I.j_tail < J) {
-                I.units[phase] = 1;
-                by_phase[phase].push_back({i, phase, -1, 0});
-                ++phase;
-                jtop = I.j_tail;
-            }
-            for (int j = jtop; j >= 1; --j, ++phase) {
-                I.units[phase] = level_units(j - 1);
-                for (int k = 0; k < I.units[phase]; ++k) by_phase[phase].push_back({i, phase, j, k});
-            }
-        }
     }
     std::vector<BatchItem> items;
     for (auto &v : by_phase) items.insert(items.end(), v.begin(), v.end());
@@ -394,14 +315,8 @@ int build_plan(dwt_gpu_batch *b)
     b->counter_bytes = sizeof(int) * (1 + size_t(b->n) * kPhases);
     b->d_counters = static_cast<int *>(c.pool.alloc(b->counter_bytes, s));
     if ((arena_floats && !b->arena) || !b->d_imgs || !b->d_items || !b->d_counters) return DWT_GPU_ENOMEM;
-    for (int i = 0; i < b->n; ++i) {
-        if (imgs[i].J == 0) continue;
-        long long p0, p1;
-        float *base = static_cast<float *>(b->arena) + scratch_off[i];
-        dense_scratch_floats(imgs[i].w, imgs[i].h, imgs[i].J, &p0, &p1);
-        imgs[i].ll[0] = base;
-        imgs[i].ll[1] = base + (imgs[i].J >= 2 ? size_t(p0) * ((imgs[i].h + 1) / 2) + 64 : 0);
-    }
+    for (int i = 0; i < b->n; ++i)
+        if (imgs[i].J > 0) set_image_scratch(imgs[i], static_cast<float *>(b->arena) + scratch_off[i]);
     if (cudaMemcpyAsync(b->d_imgs, imgs.data(), sizeof(BatchImage) * b->n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         (b->n_items && cudaMemcpyAsync(b->d_items, items.data(), sizeof(BatchItem) * b->n_items,
                                        cudaMemcpyHostToDevice, s) != cudaSuccess) ||
@@ -409,13 +324,6 @@ int build_plan(dwt_gpu_batch *b)
         return DWT_GPU_ECUDA;
 
     // the graph: zero the counters, copy zero-level images, run the kernel
-    static bool configured = false;
-    const int smem = kBatchWarps * (kStages * kStageFloats * 4 + kStages * 8);
-    if (!configured) {
-        if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-            return DWT_GPU_ECUDA;
-        configured = true;
-    }
     b->grid = std::max(1, std::min(c.sm_count * P.ctas_per_sm, (b->n_items + kBatchWarps - 1) / kBatchWarps));
     if (!b->capture && cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking) != cudaSuccess)
         return DWT_GPU_ECUDA;
@@ -427,13 +335,110 @@ int build_plan(dwt_gpu_batch *b)
             cudaMemcpy2DAsync(u.dst, u.dst_pitch_bytes, u.src, u.src_pitch_bytes, size_t(u.w) * 4, u.h,
                               cudaMemcpyDeviceToDevice, b->capture);
     }
-    if (b->n_items)
-        batch_kernel<<<b->grid, kBatchWarps * 32, smem, b->capture>>>(b->d_imgs, b->d_items, b->n_items,
-                                                                       b->d_counters, b->d_counters + 1, c.d_err);
+    if (b->n_items &&
+        launch_batch_kernel(b->grid, b->d_imgs, b->d_items, b->n_items, b->d_counters, c.d_err, b->capture) !=
+            cudaSuccess) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(b->capture, &g);
+        return DWT_GPU_ECUDA;
+    }
     if (cudaStreamEndCapture(b->capture, &b->graph) != cudaSuccess) return DWT_GPU_ECUDA;
     if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) return DWT_GPU_ECUDA;
     return DWT_GPU_OK;
 }
+
+}  // namespace
+
+namespace dwt {
+
+size_t plan_image(BatchImage &I, const dwt_gpu_batch_image &u, const dwt_gpu_batch_params &P, int i,
+                  std::vector<std::vector<BatchItem>> &by_phase)
+{
+    memset(&I, 0, sizeof(I));
+    const int lim = ceil_log2_int(u.decompose_one ? std::max(u.w, u.h) : std::min(u.w, u.h));
+    const int J = (u.j_levels < 0 || u.j_levels > lim) ? lim : u.j_levels;
+    I.src = u.src;
+    I.src_pitch = u.src_pitch_bytes / 4;
+    I.dst = u.dst;
+    I.dst_pitch = u.dst_pitch_bytes / 4;
+    I.w = u.w;
+    I.h = u.h;
+    I.J = J;
+    I.wavelet = u.wavelet;
+    I.inverse = u.inverse;
+    if (J == 0) return 0;
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(u.w, u.h, J, &p0, &p1);
+    I.llp[0] = p0;
+    I.llp[1] = p1;
+    // the first level whose band the tail item takes
+    I.j_tail = J;
+    for (int j = 0; j < J; ++j)
+        if (tail_fits(ceil_div_pow2(u.w, j), ceil_div_pow2(u.h, j), P.tail_side)) {
+            I.j_tail = j;
+            break;
+        }
+    for (int j = 0; j < J; ++j) {
+        const int w = ceil_div_pow2(u.w, j), h = ceil_div_pow2(u.h, j);
+        const int npairs = (h == 1) ? 1 : (h + 1) / 2;
+        I.n_strips[j] = ceil_div(w, kStripOut);
+        I.seg[j] = std::max(1, std::min(P.seg_pairs, npairs));
+        I.n_segs[j] = ceil_div(npairs, I.seg[j]);
+    }
+    int phase = 0;
+    auto level_units = [&](int jidx) { return I.n_strips[jidx] * I.n_segs[jidx]; };
+    if (!u.inverse) {
+        for (int j = 0; j < I.j_tail; ++j, ++phase) {
+            I.units[phase] = level_units(j);
+            for (int k = 0; k < I.units[phase]; ++k) by_phase[phase].push_back({i, phase, j, k});
+        }
+        if (I.j_tail < J) {
+            I.units[phase] = 1;
+            by_phase[phase].push_back({i, phase, -1, 0});
+        }
+    } else {
+        int jtop = J;
+        if (I.j_tail < J) {
+            I.units[phase] = 1;
+            by_phase[phase].push_back({i, phase, -1, 0});
+            ++phase;
+            jtop = I.j_tail;
+        }
+        for (int j = jtop; j >= 1; --j, ++phase) {
+            I.units[phase] = level_units(j - 1);
+            for (int k = 0; k < I.units[phase]; ++k) by_phase[phase].push_back({i, phase, j, k});
+        }
+    }
+    return sf;
+}
+
+void set_image_scratch(BatchImage &I, float *scratch)
+{
+    long long p0, p1;
+    dense_scratch_floats(I.w, I.h, I.J, &p0, &p1);
+    I.ll[0] = scratch;
+    I.ll[1] = scratch + (I.J >= 2 ? size_t(p0) * ((I.h + 1) / 2) + 64 : 0);
+}
+
+int batch_smem_bytes() { return kBatchWarps * (kStages * kStageFloats * 4 + kStages * 8); }
+
+cudaError_t launch_batch_kernel(int grid, const BatchImage *imgs, const BatchItem *items, int n_items,
+                                int *counters, int *err, cudaStream_t s)
+{
+    static bool configured = false;
+    if (!configured) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem_bytes());
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    batch_kernel<<<grid, kBatchWarps * 32, batch_smem_bytes(), s>>>(imgs, items, n_items, counters, counters + 1, err);
+    return cudaGetLastError();
+}
+
+}  // namespace dwt
+
+namespace {
 
 // --------------------------------------------------------------- autotuner
 
