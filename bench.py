@@ -443,6 +443,7 @@ def run_extras(D, torch, stream, sptr):
     for _ in range(n):
         c0dev()
     out["c0_1024_fwd_inv_device_ms"] = round((time.perf_counter() - t) / n * 1e3, 3)
+    out.update(run_signals_extra(D, torch))
     out.update(run_batch_extra(D, torch, stream, sptr))
     out.update(run_serve_extra(D, torch, SERVE_SECONDS))
     return out
@@ -526,6 +527,48 @@ def run_serve_extra(D, torch, seconds: float):
     res["c3_plain_dropin_mpx_s"] = round(px3 / (time.perf_counter() - t0) / 1e6, 1)
     res["c3_capacity_vs_plain"] = round(res["c3_x5_sustained_mpx_s"] / res["c3_plain_dropin_mpx_s"], 1)
     return res
+
+
+def run_signals_extra(D, torch, groups=8192, n=4097, lanes=8):
+    """Strided 1D lifting: 65536 AR(1) signals of 4097 samples, 8 interleaved
+    per group (element stride 32 B), CDF 9/7 forward then inverse, one batched
+    in-place launch each (dwt_gpu_1_batch_s on device memory)."""
+    from libdwt_gb300 import synth
+    from oracle import oracle as O
+    x = synth.ar1_bank(groups, n, lanes, seed=4)
+    dev = torch.from_numpy(x).cuda()
+    gs, st, count = n * lanes * 4, lanes * 4, groups * lanes
+
+    def fwd():
+        D.batch_1d("cdf97", False, dev, n, st, count, lanes, gs, 4)
+
+    def inv():
+        D.batch_1d("cdf97", True, dev, n, st, count, lanes, gs, 4)
+    fwd()
+    inv()
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fwd()
+    tf = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        inv()
+    ti = (time.perf_counter() - t0) / reps
+    samples = groups * lanes * n
+    # parity of one forward pass on a slice against the oracle
+    part = x[:64].copy()
+    ref = part.copy()
+    O.batch_1d_cdf97(ref, n, st, 64 * lanes, lanes, gs, 4, False, O.max_threads())
+    dpart = torch.from_numpy(part).cuda()
+    D.batch_1d("cdf97", False, dpart, n, st, 64 * lanes, lanes, gs, 4)
+    same = bool(np.array_equal(dpart.cpu().numpy(), ref))
+    peak = hbm_peak()[0]
+    return {"c4_signals": count, "c4_n": n, "c4_fwd_ms": round(tf * 1e3, 3), "c4_inv_ms": round(ti * 1e3, 3),
+            "c4_fwd_gsamples_s": round(samples / tf / 1e9, 2), "c4_inv_gsamples_s": round(samples / ti / 1e9, 2),
+            "c4_fwd_frac_alg": round(8 * samples / tf / 1e9 / peak, 4),
+            "c4_inv_frac_alg": round(8 * samples / ti / 1e9 / peak, 4), "c4_bit_exact_vs_oracle": same}
 
 
 def run_batch_extra(D, torch, stream, sptr, n_images=4096, j=4):

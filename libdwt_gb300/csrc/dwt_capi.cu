@@ -25,6 +25,7 @@
 #include "dwt_capi_internal.h"
 #include "dwt_coarse.cuh"
 #include "dwt_generic.cuh"
+#include "dwt_signals.cuh"
 #include "dwt_level2d.cuh"
 
 namespace dwt {
@@ -498,14 +499,34 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
     const MemKind kind = classify(base);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
     const int nl = (N + 1) / 2;
-    const long long P = align_up(N + 4, 32);
-    const int nl4 = int(align_up(nl, 4));
-    Buf in(size_t(P) * count * 4 + 256, s), out(size_t(P) * count * 4 + 256, s);
-    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
 
     // the bank's byte span (for host memory)
     const long long last = (count - 1) / group * group_stride + (count - 1) % group * (long long)lane_stride;
     const long long sb = last + (long long)(N - 1) * stride + 4;
+
+    // dense sample-interleaved groups: one CTA per group, in place
+    if (count % group == 0 && signals_fast_ok(base, N, stride, group, group_stride, lane_stride)) {
+        const long long groups = count / group;
+        void *dev = base;
+        Buf span;
+        if (!on_device) {
+            const long long gsb = (groups - 1) * group_stride + 4LL * N * group;
+            if (!span.alloc(size_t(gsb) + 16, s)) return set_error(DWT_GPU_ENOMEM);
+            CK(cudaMemcpyAsync(span.p, base, size_t(gsb), cudaMemcpyHostToDevice, s));
+            dev = span.p;
+        }
+        CK(launch_signals(wavelet, inverse, static_cast<float *>(dev), N, group, group_stride, groups, s, c.sm_count));
+        if (!on_device)
+            CK(cudaMemcpyAsync(base, span.p, size_t((groups - 1) * group_stride + 4LL * N * group),
+                               cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        return set_error(check_device_error(c));
+    }
+
+    const long long P = align_up(N + 4, 32);
+    const int nl4 = int(align_up(nl, 4));
+    Buf in(size_t(P) * count * 4 + 256, s), out(size_t(P) * count * 4 + 256, s);
+    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
     Buf span;
     const void *src = base;
     if (!on_device) {

@@ -1,0 +1,177 @@
+// Banks of interleaved 1D signals, transformed in place in one launch.
+//
+// The layout of a caller that runs dwt_cdf97_{f,i}_ex_stride_s over many
+// signals stored G to a group, sample-interleaved (sample i of signal s of
+// group g at g*group_stride + (i*G + s)*4 bytes), with L written to samples
+// [0, ceil(N/2)) and H to [ceil(N/2), N) of each signal.  One CTA owns one
+// group: it copies the group's N*G floats into shared memory with vector
+// loads, then every thread runs the lifting recurrence down a segment of one
+// signal (warmed up by the lifting latency) reading the staged samples, and
+// writes its finished L and H samples straight back to global memory.  All
+// of a group's samples are read before any is written, so in place is safe,
+// and each sample crosses HBM once each way (8 bytes per sample).
+#include "dwt_signals.cuh"
+
+#include <algorithm>
+
+namespace dwt {
+
+namespace {
+
+constexpr int kSigThreads = 256;
+
+// Forward recurrence along one signal, output samples [k0, k1) of L (and H).
+template <int NS>
+__device__ void forward_signal(const float *x, int G, int N, float *gsig, int k0, int k1, const Wavelet &W)
+{
+    constexpr int LAT = NS / 2;
+    const int nl = (N + 1) >> 1;
+    float e = 0, o = 0, o1 = 0, e1 = 0, o2 = 0;
+    for (int m = k0 - LAT; m < k1 + LAT; ++m) {
+        int ra = 2 * m, rb = 2 * m + 1;
+        if (ra < 0 || rb >= N) {
+            ra = mirror(ra, N);
+            rb = mirror(rb, N);
+        }
+        const float A = x[ra * G], B = x[rb * G];
+        float L, H;
+        if (NS == 4) {
+            const float o1n = lift(o, W.c[0], e, A);
+            const float e1n = lift(e, W.c[1], o1, o1n);
+            const float o2n = lift(o1, W.c[2], e1, e1n);
+            const float e2n = lift(e1, W.c[3], o2, o2n);
+            L = fmul(e2n, W.zeta_e);
+            H = fmul(o2n, W.zeta_o);
+            o1 = o1n; e1 = e1n; o2 = o2n;
+        } else {
+            const float o1n = lift(o, W.c[0], e, A);
+            const float e1n = lift(e, W.c[1], o1, o1n);
+            L = fmul(e1n, W.zeta_e);
+            H = fmul(o1n, W.zeta_o);
+            o1 = o1n;
+        }
+        e = A;
+        o = B;
+        const int p = m - LAT;
+        if (p >= k0) {
+            gsig[p * G] = L;
+            if (2 * p + 1 < N) gsig[(nl + p) * G] = H;
+        }
+    }
+}
+
+template <int NS>
+__device__ void inverse_signal(const float *x, int G, int N, float *gsig, int k0, int k1, const Wavelet &W)
+{
+    constexpr int LAT = NS / 2;
+    const int nl = (N + 1) >> 1;
+    float o = 0, e1 = 0, o1 = 0, e2 = 0;
+    for (int m = k0 - LAT; m < k1 + LAT; ++m) {
+        int ra = 2 * m, rb = 2 * m + 1;
+        if (ra < 0 || rb >= N) {
+            ra = mirror(ra, N);
+            rb = mirror(rb, N);
+        }
+        const float E = fmul(x[(ra >> 1) * G], W.zeta_o);
+        const float O = fmul(x[(nl + (rb >> 1)) * G], W.zeta_e);
+        float Ev, Ov;
+        if (NS == 4) {
+            const float e1n = lift(E, W.c[0], o, O);
+            const float o1n = lift(o, W.c[1], e1, e1n);
+            const float e2n = lift(e1, W.c[2], o1, o1n);
+            const float o2n = lift(o1, W.c[3], e2, e2n);
+            Ev = e2;
+            Ov = o2n;
+            e1 = e1n; o1 = o1n; e2 = e2n;
+        } else {
+            const float e1n = lift(E, W.c[0], o, O);
+            const float o1n = lift(o, W.c[1], e1, e1n);
+            Ev = e1;
+            Ov = o1n;
+            e1 = e1n;
+        }
+        o = O;
+        const int p = m - LAT;
+        if (p >= k0) {
+            gsig[(2 * p) * G] = Ev;
+            if (2 * p + 1 < N) gsig[(2 * p + 1) * G] = Ov;
+        }
+    }
+}
+
+template <int NS, bool INV>
+__global__ void __launch_bounds__(kSigThreads)
+signals_kernel(float *base, int N, int G, long long group_stride_f, long long groups, int seg, const Wavelet W)
+{
+    extern __shared__ __align__(16) float sx[];
+    const int n4 = (N * G) >> 2;  // the group block is N*G floats, a multiple of 4
+    const int per_signal = kSigThreads / G;
+    const int s = threadIdx.x % G, c = threadIdx.x / G;
+    const int npairs = (N + 1) >> 1;
+    for (long long g = blockIdx.x; g < groups; g += gridDim.x) {
+        float *gb = base + g * group_stride_f;
+        const float4 *src = reinterpret_cast<const float4 *>(gb);
+        float4 *dst4 = reinterpret_cast<float4 *>(sx);
+        for (int k = threadIdx.x; k < n4; k += kSigThreads) dst4[k] = src[k];
+        __syncthreads();
+        if (N == 1) {
+            if (c == 0) gb[s] = fmul(sx[s], INV ? W.n1_inv : W.n1_fwd);
+        } else {
+            for (int k0 = c * seg; k0 < npairs; k0 += per_signal * seg) {
+                const int k1 = min(k0 + seg, npairs);
+                if (INV)
+                    inverse_signal<NS>(sx + s, G, N, gb + s, k0, k1, W);
+                else
+                    forward_signal<NS>(sx + s, G, N, gb + s, k0, k1, W);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int NS, bool INV>
+cudaError_t launch_t(float *base, int N, int G, long long group_stride_f, long long groups, cudaStream_t s,
+                     int sm_count)
+{
+    const size_t smem = size_t(N) * G * 4;
+    static bool configured = false;
+    if (!configured) {
+        const cudaError_t e = cudaFuncSetAttribute(signals_kernel<NS, INV>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSignalsMaxSmem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const int per_signal = kSigThreads / G;
+    const int npairs = (N + 1) / 2;
+    const int seg = (npairs + per_signal - 1) / per_signal;
+    const int per_sm = int(std::max<size_t>(1, size_t(kSignalsMaxSmem) / std::max<size_t>(smem, 1)));
+    const long long grid = std::min<long long>(groups, (long long)sm_count * std::min(per_sm, 8));
+    const Wavelet W = make_wavelet(NS == 4 ? CDF97 : CDF53, INV);
+    signals_kernel<NS, INV><<<int(grid), kSigThreads, smem, s>>>(base, N, G, group_stride_f, groups, seg, W);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool signals_fast_ok(const void *base, int N, long long stride, int G, long long group_stride, long long lane_stride)
+{
+    if (N <= 0 || G <= 0 || kSigThreads % G != 0) return false;
+    if (lane_stride != 4 || stride != 4LL * G) return false;
+    if ((4LL * N * G) % 16 != 0 || (long long)N * G * 4 > kSignalsMaxSmem) return false;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || group_stride % 16 != 0) return false;
+    if (group_stride < 4LL * N * G) return false;
+    return true;
+}
+
+cudaError_t launch_signals(int wavelet, bool inverse, float *base, int N, int G, long long group_stride_bytes,
+                           long long groups, cudaStream_t s, int sm_count)
+{
+    const long long gs = group_stride_bytes / 4;
+    if (wavelet == CDF97)
+        return inverse ? launch_t<4, true>(base, N, G, gs, groups, s, sm_count)
+                       : launch_t<4, false>(base, N, G, gs, groups, s, sm_count);
+    return inverse ? launch_t<2, true>(base, N, G, gs, groups, s, sm_count)
+                   : launch_t<2, false>(base, N, G, gs, groups, s, sm_count);
+}
+
+}  // namespace dwt
