@@ -65,6 +65,10 @@ Context &ctx()
         c->device = dev ? atoi(dev) : 0;
         cudaSetDevice(c->device);
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking);
+        cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking);
+        for (auto &row : c->ev)
+            for (auto &e : row) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         cudaMalloc(&c->d_err, sizeof(int));
         cudaMemset(c->d_err, 0, sizeof(int));
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
@@ -81,6 +85,10 @@ void ctx_finish()
     cudaStreamSynchronize(g_ctx->stream);
     g_ctx->pool.release_all();
     cudaFree(g_ctx->d_err);
+    for (auto &row : g_ctx->ev)
+        for (auto &e : row) cudaEventDestroy(e);
+    cudaStreamDestroy(g_ctx->s_in);
+    cudaStreamDestroy(g_ctx->s_out);
     cudaStreamDestroy(g_ctx->stream);
     delete g_ctx;
     g_ctx = nullptr;
@@ -176,33 +184,75 @@ static int coarse_level(int W, int H, int J)
     return J;
 }
 
-cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long long out_pitch, int W,
-                          int H, int J, int wavelet, float *scratch, cudaStream_t s, int *err,
-                          int seg_hint)
+// Descriptor of forward level j (LL_j -> LL_{j+1} in scratch, or in `out`
+// for the last level, and the three detail bands in `out`).
+static LevelDesc fwd_desc(const float *in, long long in_pitch, float *out, long long out_pitch, int W, int H,
+                          int J, int j, float *const buf[2], const long long p[2])
 {
-    long long p[2];
+    const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
+    const int wd = (w + 1) / 2, hd = (h + 1) / 2;
+    LevelDesc d{};
+    d.w = w;
+    d.h = h;
+    d.in[0] = j == 0 ? in : buf[(j - 1) % 2];
+    d.in_pitch[0] = j == 0 ? in_pitch : p[(j - 1) % 2];
+    if (j == J - 1) {
+        d.out[0] = out;
+        d.out_pitch[0] = out_pitch;
+    } else {
+        d.out[0] = buf[j % 2];
+        d.out_pitch[0] = p[j % 2];
+    }
+    d.out[1] = out + wd;
+    d.out[2] = out + hd * out_pitch;
+    d.out[3] = out + hd * out_pitch + wd;
+    d.out_pitch[1] = d.out_pitch[2] = d.out_pitch[3] = out_pitch;
+    return d;
+}
+
+// Descriptor of inverse level j (LL_j and the details of level j -> LL_{j-1}).
+static LevelDesc inv_desc(const float *in, long long in_pitch, float *out, long long out_pitch, int W, int H,
+                          int J, int j, float *const buf[2], const long long p[2])
+{
+    const int w = ceil_div_pow2(W, j - 1), h = ceil_div_pow2(H, j - 1);
+    const int ws = (w + 1) / 2, hs = (h + 1) / 2;
+    LevelDesc d{};
+    d.w = w;
+    d.h = h;
+    d.in[0] = j == J ? in : buf[(j - 1) % 2];
+    d.in_pitch[0] = j == J ? in_pitch : p[(j - 1) % 2];
+    d.in[1] = in + ws;
+    d.in[2] = in + hs * in_pitch;
+    d.in[3] = in + hs * in_pitch + ws;
+    d.in_pitch[1] = d.in_pitch[2] = d.in_pitch[3] = in_pitch;
+    if (j == 1) {
+        d.out[0] = out;
+        d.out_pitch[0] = out_pitch;
+    } else {
+        d.out[0] = buf[(j - 2) % 2];
+        d.out_pitch[0] = p[(j - 2) % 2];
+    }
+    return d;
+}
+
+static void scratch_frames(int W, int H, int J, float *scratch, float *buf[2], long long p[2])
+{
     dense_scratch_floats(W, H, J, &p[0], &p[1]);
-    float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
-    const int j0 = coarse_level(W, H, J);
-    for (int j = 0; j < j0; ++j) {
-        const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
-        const int wd = (w + 1) / 2, hd = (h + 1) / 2;
-        LevelDesc d{};
-        d.w = w;
-        d.h = h;
-        d.in[0] = j == 0 ? in : buf[(j - 1) % 2];
-        d.in_pitch[0] = j == 0 ? in_pitch : p[(j - 1) % 2];
-        if (j == J - 1) {
-            d.out[0] = out;
-            d.out_pitch[0] = out_pitch;
-        } else {
-            d.out[0] = buf[j % 2];
-            d.out_pitch[0] = p[j % 2];
-        }
-        d.out[1] = out + wd;
-        d.out[2] = out + hd * out_pitch;
-        d.out[3] = out + hd * out_pitch + wd;
-        d.out_pitch[1] = d.out_pitch[2] = d.out_pitch[3] = out_pitch;
+    buf[0] = scratch;
+    buf[1] = scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0);
+}
+
+// Forward levels j_begin .. J-1 (the coarse kernel takes over once the band fits).
+static cudaError_t dense_forward_levels(const float *in, long long in_pitch, float *out, long long out_pitch,
+                                        int W, int H, int J, int j_begin, int wavelet, float *scratch,
+                                        cudaStream_t s, int *err, int seg_hint)
+{
+    float *buf[2];
+    long long p[2];
+    scratch_frames(W, H, J, scratch, buf, p);
+    const int j0 = std::max(coarse_level(W, H, J), j_begin);
+    for (int j = j_begin; j < j0; ++j) {
+        LevelDesc d = fwd_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
         plan_level(d, seg_hint);
         cudaError_t e = launch_level(d, wavelet, false, s, err);
         if (e != cudaSuccess) return e;
@@ -216,47 +266,178 @@ cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long 
     return cudaSuccess;
 }
 
-cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long long out_pitch, int W,
-                          int H, int J, int wavelet, float *scratch, cudaStream_t s, int *err,
-                          int seg_hint)
+// Inverse levels J .. j_end (j_end >= 1).
+static cudaError_t dense_inverse_levels(const float *in, long long in_pitch, float *out, long long out_pitch,
+                                        int W, int H, int J, int j_end, int wavelet, float *scratch,
+                                        cudaStream_t s, int *err, int seg_hint)
 {
+    float *buf[2];
     long long p[2];
-    dense_scratch_floats(W, H, J, &p[0], &p[1]);
-    float *buf[2] = {scratch, scratch + (J >= 2 ? size_t(p[0]) * ((H + 1) / 2) + 64 : 0)};
+    scratch_frames(W, H, J, scratch, buf, p);
     const int j0 = coarse_level(W, H, J);
     int jtop = J;  // level whose LL the next level kernel reads
-    if (j0 < J) {
+    if (j0 < J && j0 >= j_end - 1) {
         float *dst = j0 == 0 ? out : buf[(j0 - 1) % 2];
         const long long dp = j0 == 0 ? out_pitch : p[(j0 - 1) % 2];
-        cudaError_t e = launch_coarse(true, in, in_pitch, ceil_div_pow2(W, j0), ceil_div_pow2(H, j0),
-                                      J - j0, dst, dp, wavelet, s);
+        cudaError_t e = launch_coarse(true, in, in_pitch, ceil_div_pow2(W, j0), ceil_div_pow2(H, j0), J - j0,
+                                      dst, dp, wavelet, s);
         if (e != cudaSuccess) return e;
         jtop = j0;
     }
-    for (int j = jtop; j >= 1; --j) {
-        const int w = ceil_div_pow2(W, j - 1), h = ceil_div_pow2(H, j - 1);
-        const int ws = (w + 1) / 2, hs = (h + 1) / 2;
-        LevelDesc d{};
-        d.w = w;
-        d.h = h;
-        d.in[0] = j == J ? in : buf[(j - 1) % 2];
-        d.in_pitch[0] = j == J ? in_pitch : p[(j - 1) % 2];
-        d.in[1] = in + ws;
-        d.in[2] = in + hs * in_pitch;
-        d.in[3] = in + hs * in_pitch + ws;
-        d.in_pitch[1] = d.in_pitch[2] = d.in_pitch[3] = in_pitch;
-        if (j == 1) {
-            d.out[0] = out;
-            d.out_pitch[0] = out_pitch;
-        } else {
-            d.out[0] = buf[(j - 2) % 2];
-            d.out_pitch[0] = p[(j - 2) % 2];
-        }
+    for (int j = jtop; j >= j_end; --j) {
+        LevelDesc d = inv_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
         plan_level(d, seg_hint);
         cudaError_t e = launch_level(d, wavelet, true, s, err);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t dense_forward(const float *in, long long in_pitch, float *out, long long out_pitch, int W, int H,
+                          int J, int wavelet, float *scratch, cudaStream_t s, int *err, int seg_hint)
+{
+    return dense_forward_levels(in, in_pitch, out, out_pitch, W, H, J, 0, wavelet, scratch, s, err, seg_hint);
+}
+
+cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long long out_pitch, int W, int H,
+                          int J, int wavelet, float *scratch, cudaStream_t s, int *err, int seg_hint)
+{
+    return dense_inverse_levels(in, in_pitch, out, out_pitch, W, H, J, 1, wavelet, scratch, s, err, seg_hint);
+}
+
+// ------------------------------------------------- pipelined host frames
+
+// A dense frame in host memory is copied in, transformed and copied out in
+// row bands on three streams, so that the copies in and out (full duplex over
+// the host link) overlap each other and the kernels.  Forward: band b of the
+// input rows is copied in, the level-0 segments whose rows (with the lifting
+// warm-up) are then present run, and their finished detail rows (HL of those
+// rows, LH and HH of the matching lower rows) are copied out at once; the
+// coarser levels follow on the small LL band and the top-left quadrant is
+// copied out last.  Inverse: the top-left quadrant (LL1 and every coarser
+// band) comes first, levels J..2 run, then level 1 runs band by band as its
+// detail rows arrive and its output rows leave.
+constexpr int kBands = 16;
+constexpr long long kPipelineMinPixels = 1LL << 22;
+
+static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
+{
+    cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
+    const long long P = align_up(W, 32);
+    Buf in(size_t(P) * H * 4 + 256, s), out(size_t(P) * H * 4 + 256, s);
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(W, H, J, &p0, &p1);
+    Buf scratch(sf * 4 + 256, s);
+    if (!in.p || !out.p || (sf && !scratch.p)) return set_error(DWT_GPU_ENOMEM);
+    float *buf[2];
+    long long p[2];
+    scratch_frames(W, H, J, scratch.f(), buf, p);
+    // the pool may hand out blocks last used on `s`: let the copy streams wait
+    CK(cudaEventRecord(c.ev[0][0], s));
+    CK(cudaStreamWaitEvent(si, c.ev[0][0], 0));
+    CK(cudaStreamWaitEvent(so, c.ev[0][0], 0));
+
+    const int LAT = wavelet == CDF97 ? 2 : 1;
+    const int wd = (W + 1) / 2, hd = (H + 1) / 2, hh = H / 2;
+    LevelDesc d0 = fwd_desc(in.f(), P, out.f(), P, W, H, J, 0, buf, p);
+    plan_level(d0, 0);
+    const int npairs = (H + 1) / 2, seg = d0.seg_pairs, nsegs = d0.n_segs;
+    const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
+    int rows_in = 0, b = 0;
+    for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
+        const int se = std::min(nsegs, sb + per_band);
+        const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
+        const int need = std::min(H, 2 * k1 + 2 * LAT);
+        if (need > rows_in) {
+            CK(cudaMemcpy2DAsync(in.f() + rows_in * P, P * 4, host + rows_in * sx, sx, size_t(W) * 4, need - rows_in,
+                                 cudaMemcpyHostToDevice, si));
+            rows_in = need;
+        }
+        CK(cudaEventRecord(c.ev[0][b], si));
+        CK(cudaStreamWaitEvent(s, c.ev[0][b], 0));
+        LevelDesc d = d0;
+        d.seg_base = sb;
+        d.n_segs = se - sb;
+        CK(launch_level(d, wavelet, false, s, c.d_err));
+        CK(cudaEventRecord(c.ev[1][b], s));
+        CK(cudaStreamWaitEvent(so, c.ev[1][b], 0));
+        if (W > wd)
+            CK(cudaMemcpy2DAsync(host + k0 * sx + wd * 4LL, sx, out.f() + k0 * P + wd, P * 4, size_t(W - wd) * 4,
+                                 k1 - k0, cudaMemcpyDeviceToHost, so));
+        const int hk1 = std::min(k1, hh);
+        if (hk1 > k0)
+            CK(cudaMemcpy2DAsync(host + (hd + k0) * sx, sx, out.f() + (hd + k0) * P, P * 4, size_t(W) * 4, hk1 - k0,
+                                 cudaMemcpyDeviceToHost, so));
+    }
+    if (J > 1) CK(dense_forward_levels(in.f(), P, out.f(), P, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
+    CK(cudaEventRecord(c.ev[0][63], s));
+    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
+    CK(cudaMemcpy2DAsync(host, sx, out.f(), P * 4, size_t(wd) * 4, hd, cudaMemcpyDeviceToHost, so));
+    // buffers go back to the pool on `s`: order `s` after the copy-out
+    CK(cudaEventRecord(c.ev[1][63], so));
+    CK(cudaStreamWaitEvent(s, c.ev[1][63], 0));
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
+{
+    cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
+    const long long P = align_up(W, 32);
+    Buf in(size_t(P) * H * 4 + 256, s), out(size_t(P) * H * 4 + 256, s);
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(W, H, J, &p0, &p1);
+    Buf scratch(sf * 4 + 256, s);
+    if (!in.p || !out.p || (sf && !scratch.p)) return set_error(DWT_GPU_ENOMEM);
+    float *buf[2];
+    long long p[2];
+    scratch_frames(W, H, J, scratch.f(), buf, p);
+    CK(cudaEventRecord(c.ev[0][0], s));
+    CK(cudaStreamWaitEvent(si, c.ev[0][0], 0));
+    CK(cudaStreamWaitEvent(so, c.ev[0][0], 0));
+
+    const int LAT = wavelet == CDF97 ? 2 : 1;
+    const int ws = (W + 1) / 2, hs = (H + 1) / 2, hh = H / 2;
+    // the top-left quadrant first: LL1 and every coarser band
+    CK(cudaMemcpy2DAsync(in.f(), P * 4, host, sx, size_t(ws) * 4, hs, cudaMemcpyHostToDevice, si));
+    CK(cudaEventRecord(c.ev[0][1], si));
+    CK(cudaStreamWaitEvent(s, c.ev[0][1], 0));
+    if (J > 1) CK(dense_inverse_levels(in.f(), P, out.f(), P, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
+
+    LevelDesc d1 = inv_desc(in.f(), P, out.f(), P, W, H, J, 1, buf, p);
+    plan_level(d1, 0);
+    const int npairs = (H + 1) / 2, seg = d1.seg_pairs, nsegs = d1.n_segs;
+    const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
+    int top_in = 0, bot_in = 0, b = 2;
+    for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
+        const int se = std::min(nsegs, sb + per_band);
+        const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
+        // band rows read by output pairs up to k1 - 1 (with the warm-up)
+        const int need_top = std::min(hs, k1 + LAT), need_bot = std::min(hh, k1 + LAT);
+        if (need_top > top_in && W > ws)
+            CK(cudaMemcpy2DAsync(in.f() + top_in * P + ws, P * 4, host + top_in * sx + ws * 4LL, sx,
+                                 size_t(W - ws) * 4, need_top - top_in, cudaMemcpyHostToDevice, si));
+        if (need_bot > bot_in)
+            CK(cudaMemcpy2DAsync(in.f() + (hs + bot_in) * P, P * 4, host + (hs + bot_in) * sx, sx, size_t(W) * 4,
+                                 need_bot - bot_in, cudaMemcpyHostToDevice, si));
+        top_in = std::max(top_in, need_top);
+        bot_in = std::max(bot_in, need_bot);
+        CK(cudaEventRecord(c.ev[0][b], si));
+        CK(cudaStreamWaitEvent(s, c.ev[0][b], 0));
+        LevelDesc d = d1;
+        d.seg_base = sb;
+        d.n_segs = se - sb;
+        CK(launch_level(d, wavelet, true, s, c.d_err));
+        CK(cudaEventRecord(c.ev[1][b], s));
+        CK(cudaStreamWaitEvent(so, c.ev[1][b], 0));
+        const int r0 = 2 * k0, r1 = std::min(H, 2 * k1);
+        CK(cudaMemcpy2DAsync(host + r0 * sx, sx, out.f() + r0 * P, P * 4, size_t(W) * 4, r1 - r0,
+                             cudaMemcpyDeviceToHost, so));
+    }
+    CK(cudaEventRecord(c.ev[1][63], so));
+    CK(cudaStreamWaitEvent(s, c.ev[1][63], 0));
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
 }
 
 // ------------------------------------------------------------ 2D driver
@@ -324,6 +505,15 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     const long long P = align_up(ox, 32);  // compact pitch in floats
     // a single-row frame may carry any row stride; 2D copies want pitch >= width
     const long long csx = oy == 1 ? std::max<long long>(sx, 4LL * ox) : sx;
+
+    // large dense host frames: banded copy/compute overlap
+    {
+        const bool rows4h = sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
+        if (!on_device && dense && rows4h && (long long)ox * oy >= kPipelineMinPixels && oy >= 64) {
+            return inverse ? pipelined_inverse(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J)
+                           : pipelined_forward(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J);
+        }
+    }
 
     // 1. stage into IN
     Buf in(size_t(P) * oy * 4 + 256, s);

@@ -17,6 +17,8 @@ struct Context {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t s_in = nullptr, s_out = nullptr;  // copy streams of the pipelined host path
+    cudaEvent_t ev[2][64] = {};                      // band events of the pipelined host path
     int *d_err = nullptr;
     Pool pool;
     std::mutex call_mu;  // drop-in calls share `stream`

@@ -34,7 +34,7 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err)
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
     for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
-        const int strip = u % D.n_strips, seg = u / D.n_strips;
+        const int strip = u % D.n_strips, seg = D.seg_base + u / D.n_strips;
         if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch)) break;
     }
 }

@@ -32,6 +32,7 @@ constexpr int kSmemBytes = kWarpsPerCta * (kStages * kStageFloats * 4 + kStages 
 struct LevelDesc {
     int w, h;
     int n_strips, seg_pairs, n_segs;
+    int seg_base;  // first segment of this launch (a launch may cover a sub-range)
     int rows_only;
     const float *in[4];
     long long in_pitch[4];

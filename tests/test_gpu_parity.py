@@ -152,3 +152,24 @@ def test_roundtrip_within_reference_tolerance(D, torch):
         j = D.transform2(buf, wav, "f", W * 4, 4, (W, H), (W, H), -1)
         D.transform2(buf, wav, "i", W * 4, 4, (W, H), (W, H), j)
         assert np.all(np.isfinite(buf)) and np.abs(buf - img).max() <= 1e-3
+
+
+def test_large_host_frames_pipelined(D, torch):
+    """Host frames of 4 Mpx and more take the banded copy/compute pipeline;
+    outputs stay bit-identical to the oracle (pinned and pageable memory)."""
+    rng = np.random.default_rng(17)
+    for (w, h, pinned) in [(2500, 2000, True), (2049, 2051, False), (4096, 1024, True)]:
+        img = rng.integers(0, 256, size=(h, w)).astype(np.float32)
+        for wav in ("cdf97", "cdf53"):
+            for j in (-1, 1, 3):
+                ref_f, jr = O.transform2_dense(img, wav, "f", j, 0, "s", O.max_threads())
+                ref_i, _ = O.transform2_dense(ref_f, wav, "i", jr, 0, "s", O.max_threads())
+                buf = torch.from_numpy(img.copy())
+                if pinned:
+                    buf = buf.pin_memory()
+                arr = buf.numpy()
+                jj = D.transform2(arr, wav, "f", w * 4, 4, (w, h), (w, h), j)
+                assert jj == jr
+                assert np.array_equal(arr, ref_f), (w, h, wav, j, "f")
+                D.transform2(arr, wav, "i", w * 4, 4, (w, h), (w, h), jr)
+                assert np.array_equal(arr, ref_i), (w, h, wav, j, "i")
