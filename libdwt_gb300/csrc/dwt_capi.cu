@@ -20,6 +20,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/libdwt.h"
 #include "dwt_capi_internal.h"
@@ -320,6 +321,14 @@ cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long 
 constexpr int kBands = 16;
 constexpr long long kPipelineMinPixels = 1LL << 22;
 
+// A copy out to host rows [r0, r1) (columns [c0, c1)) waits until the copy
+// in has read those host rows: the caller's frame is both input and output.
+struct HostOut {
+    int r0, r1, c0, c1;  // host rows / columns
+    const float *src;    // device address of (r0, c0)
+    int ev;              // compute event it follows
+};
+
 static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
 {
     cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
@@ -333,9 +342,9 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
     // the pool may hand out blocks last used on `s`: let the copy streams wait
-    CK(cudaEventRecord(c.ev[0][0], s));
-    CK(cudaStreamWaitEvent(si, c.ev[0][0], 0));
-    CK(cudaStreamWaitEvent(so, c.ev[0][0], 0));
+    CK(cudaEventRecord(c.ev[0][63], s));
+    CK(cudaStreamWaitEvent(si, c.ev[0][63], 0));
+    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
 
     const int LAT = wavelet == CDF97 ? 2 : 1;
     const int wd = (W + 1) / 2, hd = (H + 1) / 2, hh = H / 2;
@@ -343,7 +352,23 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     plan_level(d0, 0);
     const int npairs = (H + 1) / 2, seg = d0.seg_pairs, nsegs = d0.n_segs;
     const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
-    int rows_in = 0, b = 0;
+    std::vector<HostOut> pending;
+    int rows_in = 0, b = 0, last_in_ev = -1;
+    auto flush = [&](bool all) -> cudaError_t {
+        size_t k = 0;
+        for (; k < pending.size(); ++k) {
+            const HostOut &o = pending[k];
+            if (!all && o.r1 > rows_in) break;
+            cudaError_t e = cudaStreamWaitEvent(so, c.ev[1][o.ev], 0);
+            if (e == cudaSuccess && last_in_ev >= 0) e = cudaStreamWaitEvent(so, c.ev[0][last_in_ev], 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(host + o.r0 * sx + o.c0 * 4LL, sx, o.src, P * 4, size_t(o.c1 - o.c0) * 4,
+                                      o.r1 - o.r0, cudaMemcpyDeviceToHost, so);
+            if (e != cudaSuccess) return e;
+        }
+        pending.erase(pending.begin(), pending.begin() + k);
+        return cudaSuccess;
+    };
     for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
         const int se = std::min(nsegs, sb + per_band);
         const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
@@ -354,28 +379,29 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
             rows_in = need;
         }
         CK(cudaEventRecord(c.ev[0][b], si));
+        last_in_ev = b;
         CK(cudaStreamWaitEvent(s, c.ev[0][b], 0));
         LevelDesc d = d0;
         d.seg_base = sb;
         d.n_segs = se - sb;
         CK(launch_level(d, wavelet, false, s, c.d_err));
         CK(cudaEventRecord(c.ev[1][b], s));
-        CK(cudaStreamWaitEvent(so, c.ev[1][b], 0));
-        if (W > wd)
-            CK(cudaMemcpy2DAsync(host + k0 * sx + wd * 4LL, sx, out.f() + k0 * P + wd, P * 4, size_t(W - wd) * 4,
-                                 k1 - k0, cudaMemcpyDeviceToHost, so));
+        // HL of rows [k0, k1) and LH, HH of rows [hd + k0, hd + k1)
+        if (W > wd) pending.push_back({k0, k1, wd, W, out.f() + k0 * P + wd, b});
         const int hk1 = std::min(k1, hh);
-        if (hk1 > k0)
-            CK(cudaMemcpy2DAsync(host + (hd + k0) * sx, sx, out.f() + (hd + k0) * P, P * 4, size_t(W) * 4, hk1 - k0,
-                                 cudaMemcpyDeviceToHost, so));
+        if (hk1 > k0) pending.push_back({hd + k0, hd + hk1, 0, W, out.f() + (hd + k0) * P, b});
+        std::stable_sort(pending.begin(), pending.end(),
+                         [](const HostOut &x, const HostOut &y) { return x.r1 < y.r1; });
+        CK(flush(false));
     }
+    CK(flush(true));
     if (J > 1) CK(dense_forward_levels(in.f(), P, out.f(), P, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
-    CK(cudaEventRecord(c.ev[0][63], s));
-    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
+    CK(cudaEventRecord(c.ev[1][63], s));
+    CK(cudaStreamWaitEvent(so, c.ev[1][63], 0));
     CK(cudaMemcpy2DAsync(host, sx, out.f(), P * 4, size_t(wd) * 4, hd, cudaMemcpyDeviceToHost, so));
     // buffers go back to the pool on `s`: order `s` after the copy-out
-    CK(cudaEventRecord(c.ev[1][63], so));
-    CK(cudaStreamWaitEvent(s, c.ev[1][63], 0));
+    CK(cudaEventRecord(c.ev[0][62], so));
+    CK(cudaStreamWaitEvent(s, c.ev[0][62], 0));
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));
 }
@@ -392,28 +418,32 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
     float *buf[2];
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
-    CK(cudaEventRecord(c.ev[0][0], s));
-    CK(cudaStreamWaitEvent(si, c.ev[0][0], 0));
-    CK(cudaStreamWaitEvent(so, c.ev[0][0], 0));
+    CK(cudaEventRecord(c.ev[0][63], s));
+    CK(cudaStreamWaitEvent(si, c.ev[0][63], 0));
+    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
 
     const int LAT = wavelet == CDF97 ? 2 : 1;
     const int ws = (W + 1) / 2, hs = (H + 1) / 2, hh = H / 2;
     // the top-left quadrant first: LL1 and every coarser band
     CK(cudaMemcpy2DAsync(in.f(), P * 4, host, sx, size_t(ws) * 4, hs, cudaMemcpyHostToDevice, si));
-    CK(cudaEventRecord(c.ev[0][1], si));
-    CK(cudaStreamWaitEvent(s, c.ev[0][1], 0));
+    CK(cudaEventRecord(c.ev[0][0], si));
+    CK(cudaStreamWaitEvent(s, c.ev[0][0], 0));
     if (J > 1) CK(dense_inverse_levels(in.f(), P, out.f(), P, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
 
     LevelDesc d1 = inv_desc(in.f(), P, out.f(), P, W, H, J, 1, buf, p);
     plan_level(d1, 0);
     const int npairs = (H + 1) / 2, seg = d1.seg_pairs, nsegs = d1.n_segs;
     const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
-    int top_in = 0, bot_in = 0, b = 2;
+    int top_in = 0, bot_in = 0, b = 1;
     for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
         const int se = std::min(nsegs, sb + per_band);
         const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
-        // band rows read by output pairs up to k1 - 1 (with the warm-up)
-        const int need_top = std::min(hs, k1 + LAT), need_bot = std::min(hh, k1 + LAT);
+        const int r0 = 2 * k0, r1 = std::min(H, 2 * k1);
+        // the band rows the output pairs read (with the warm-up), and at least
+        // every input row the band's output rows overwrite on the host
+        int need_top = std::min(hs, k1 + LAT), need_bot = std::min(hh, k1 + LAT);
+        need_top = std::max(need_top, std::min(hs, r1));
+        need_bot = std::max(need_bot, std::min(hh, r1 - hs));
         if (need_top > top_in && W > ws)
             CK(cudaMemcpy2DAsync(in.f() + top_in * P + ws, P * 4, host + top_in * sx + ws * 4LL, sx,
                                  size_t(W - ws) * 4, need_top - top_in, cudaMemcpyHostToDevice, si));
@@ -429,13 +459,14 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
         d.n_segs = se - sb;
         CK(launch_level(d, wavelet, true, s, c.d_err));
         CK(cudaEventRecord(c.ev[1][b], s));
+        // the output rows overwrite host rows whose input is already read
         CK(cudaStreamWaitEvent(so, c.ev[1][b], 0));
-        const int r0 = 2 * k0, r1 = std::min(H, 2 * k1);
+        CK(cudaStreamWaitEvent(so, c.ev[0][b], 0));
         CK(cudaMemcpy2DAsync(host + r0 * sx, sx, out.f() + r0 * P, P * 4, size_t(W) * 4, r1 - r0,
                              cudaMemcpyDeviceToHost, so));
     }
-    CK(cudaEventRecord(c.ev[1][63], so));
-    CK(cudaStreamWaitEvent(s, c.ev[1][63], 0));
+    CK(cudaEventRecord(c.ev[0][62], so));
+    CK(cudaStreamWaitEvent(s, c.ev[0][62], 0));
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));
 }
