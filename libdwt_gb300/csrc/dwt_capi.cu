@@ -736,7 +736,8 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
             CK(cudaMemcpyAsync(span.p, base, size_t(gsb), cudaMemcpyHostToDevice, s));
             dev = span.p;
         }
-        CK(launch_signals(wavelet, inverse, static_cast<float *>(dev), N, group, group_stride, groups, s, c.sm_count));
+        CK(launch_signals(wavelet, inverse, static_cast<float *>(dev), N, group, group_stride, groups, s, c.sm_count,
+                          c.d_err));
         if (!on_device)
             CK(cudaMemcpyAsync(base, span.p, size_t((groups - 1) * group_stride + 4LL * N * group),
                                cudaMemcpyDeviceToHost, s));

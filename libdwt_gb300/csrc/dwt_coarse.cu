@@ -29,7 +29,7 @@ coarse_forward_kernel(const float *in, long long in_pitch, int w0, int h0, int l
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ float sm[];
-    const int P = w0 + 1, PT = h0 + 1;
+    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
     float *A = sm, *B = sm + P * h0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
@@ -57,7 +57,7 @@ coarse_inverse_kernel(const float *in, long long in_pitch, int w0, int h0, int l
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ float sm[];
-    const int P = w0 + 1, PT = h0 + 1;
+    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
     float *A = sm, *B = sm + P * h0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
@@ -102,7 +102,7 @@ cudaError_t launch_coarse(bool inverse, const float *in, long long in_pitch, int
     }
     if (!coarse_fits(w, h)) return cudaErrorInvalidValue;
     const Wavelet W = make_wavelet(wavelet, inverse);
-    const size_t smem = size_t(4) * ((w + 1) * h + (h + 1) * w);
+    const size_t smem = size_t(4) * (coarse_pitch(w) * h + coarse_pitch(h) * w);
     if (wavelet == CDF97) {
         if (inverse)
             coarse_inverse_kernel<4><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);

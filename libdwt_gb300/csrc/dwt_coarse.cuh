@@ -5,15 +5,16 @@
 
 namespace dwt {
 
-// Shared memory of the coarse kernel: the band (pitch w+1) and its
-// transpose (pitch h+1).
+// Shared memory of the coarse kernel: the band and its transpose, line
+// pitches rounded up to 4 floats (16-byte line starts).
 constexpr int kCoarseSmem = 200 * 1024;
+__host__ __device__ inline int coarse_pitch(int n) { return (n + 3) & ~3; }
 // Bands the coarse kernel takes: lines of at most 252 samples (one warp), and
 // both buffers within kCoarseSmem.
 __host__ __device__ inline bool coarse_fits(int w, int h)
 {
     return w >= 1 && h >= 1 && w <= 252 && h <= 252 &&
-           4LL * ((long long)(w + 1) * h + (long long)(h + 1) * w) <= kCoarseSmem;
+           4LL * ((long long)coarse_pitch(w) * h + (long long)coarse_pitch(h) * w) <= kCoarseSmem;
 }
 
 // Forward: `in` is the w x h LL band entering level j0; runs `levels` levels

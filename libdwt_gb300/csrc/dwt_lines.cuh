@@ -81,11 +81,21 @@ __device__ __forceinline__ void pass_forward(const float *src, int ls, float *ds
         ld[k] = mirror(i, n);
         st[k] = i < n ? ((k & 1) ? nd + (i >> 1) : (i >> 1)) * dp : -1;
     }
+    // lanes whose 8 samples lie inside the line read them as two 16-byte
+    // loads (line pitches are multiples of 4 floats)
+    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0);
     for (int l = warp; l < nl; l += nwarps) {
         const float *line = src + l * ls;
         float x[kV];
+        if (vec) {
+            const float4 a = *reinterpret_cast<const float4 *>(line + kV * lane);
+            const float4 b = *reinterpret_cast<const float4 *>(line + kV * lane + 4);
+            x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+            x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+        } else {
 #pragma unroll
-        for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+            for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+        }
         line_forward<NS>(x, W, lane);
 #pragma unroll
         for (int k = 0; k < kV; ++k)
@@ -112,11 +122,21 @@ __device__ __forceinline__ void pass_inverse(const float *src, int ls, float *ds
         ld[k] = (m & 1) ? nd + (m >> 1) : (m >> 1);
         st[k] = i < n ? i * dp : -1;
     }
+    // lanes whose 8 samples lie inside the line read their 4 L and 4 H
+    // samples as two 16-byte loads when both halves start 16-byte aligned
+    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0) && ((nd & 3) == 0);
     for (int l = warp; l < nl; l += nwarps) {
         const float *line = src + l * ls;
         float x[kV];
+        if (vec) {
+            const float4 a = *reinterpret_cast<const float4 *>(line + 4 * lane);
+            const float4 b = *reinterpret_cast<const float4 *>(line + nd + 4 * lane);
+            x[0] = a.x; x[1] = b.x; x[2] = a.y; x[3] = b.y;
+            x[4] = a.z; x[5] = b.z; x[6] = a.w; x[7] = b.w;
+        } else {
 #pragma unroll
-        for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+            for (int k = 0; k < kV; ++k) x[k] = line[ld[k]];
+        }
         line_inverse<NS>(x, W, lane);
 #pragma unroll
         for (int k = 0; k < kV; ++k)

@@ -18,7 +18,8 @@ namespace dwt {
 
 namespace {
 
-constexpr int kSigThreads = 256;
+constexpr int kSigThreads = 512;
+constexpr uint32_t kBulkChunk = 32768;  // bytes per bulk copy
 
 // Forward recurrence along one signal, output samples [k0, k1) of L (and H).
 template <int NS>
@@ -101,19 +102,37 @@ __device__ void inverse_signal(const float *x, int G, int N, float *gsig, int k0
 
 template <int NS, bool INV>
 __global__ void __launch_bounds__(kSigThreads)
-signals_kernel(float *base, int N, int G, long long group_stride_f, long long groups, int seg, const Wavelet W)
+signals_kernel(float *base, int N, int G, long long group_stride_f, long long groups, int seg, const Wavelet W,
+               int *err)
 {
-    extern __shared__ __align__(16) float sx[];
-    const int n4 = (N * G) >> 2;  // the group block is N*G floats, a multiple of 4
+    extern __shared__ __align__(128) float sx[];
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t bytes = uint32_t(N) * uint32_t(G) * 4u;  // a multiple of 16
     const int per_signal = kSigThreads / G;
     const int s = threadIdx.x % G, c = threadIdx.x / G;
     const int npairs = (N + 1) >> 1;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    // the TMA engine stages the whole group block; one mbarrier phase per group
+    auto stage = [&](long long g) {
+        const char *src = reinterpret_cast<const char *>(base + g * group_stride_f);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar, bytes);
+        for (uint32_t o = 0; o < bytes; o += kBulkChunk)
+            bulk_g2s(reinterpret_cast<char *>(sx) + o, src + o, min(kBulkChunk, bytes - o), &bar);
+    };
+    if (threadIdx.x == 0 && blockIdx.x < groups) stage(blockIdx.x);
     for (long long g = blockIdx.x; g < groups; g += gridDim.x) {
         float *gb = base + g * group_stride_f;
-        const float4 *src = reinterpret_cast<const float4 *>(gb);
-        float4 *dst4 = reinterpret_cast<float4 *>(sx);
-        for (int k = threadIdx.x; k < n4; k += kSigThreads) dst4[k] = src[k];
-        __syncthreads();
+        if (!mbar_wait_bounded(&bar, phase)) {
+            if (threadIdx.x == 0) atomicCAS(err, 0, kErrWaitTimeout);
+            return;
+        }
+        phase ^= 1u;
         if (N == 1) {
             if (c == 0) gb[s] = fmul(sx[s], INV ? W.n1_inv : W.n1_fwd);
         } else {
@@ -125,13 +144,14 @@ signals_kernel(float *base, int N, int G, long long group_stride_f, long long gr
                     forward_signal<NS>(sx + s, G, N, gb + s, k0, k1, W);
             }
         }
-        __syncthreads();
+        __syncthreads();  // every thread is done with the staged block
+        if (threadIdx.x == 0 && g + gridDim.x < groups) stage(g + gridDim.x);
     }
 }
 
 template <int NS, bool INV>
 cudaError_t launch_t(float *base, int N, int G, long long group_stride_f, long long groups, cudaStream_t s,
-                     int sm_count)
+                     int sm_count, int *err)
 {
     const size_t smem = size_t(N) * G * 4;
     static bool configured = false;
@@ -147,7 +167,7 @@ cudaError_t launch_t(float *base, int N, int G, long long group_stride_f, long l
     const int per_sm = int(std::max<size_t>(1, size_t(kSignalsMaxSmem) / std::max<size_t>(smem, 1)));
     const long long grid = std::min<long long>(groups, (long long)sm_count * std::min(per_sm, 8));
     const Wavelet W = make_wavelet(NS == 4 ? CDF97 : CDF53, INV);
-    signals_kernel<NS, INV><<<int(grid), kSigThreads, smem, s>>>(base, N, G, group_stride_f, groups, seg, W);
+    signals_kernel<NS, INV><<<int(grid), kSigThreads, smem, s>>>(base, N, G, group_stride_f, groups, seg, W, err);
     return cudaGetLastError();
 }
 
@@ -164,14 +184,14 @@ bool signals_fast_ok(const void *base, int N, long long stride, int G, long long
 }
 
 cudaError_t launch_signals(int wavelet, bool inverse, float *base, int N, int G, long long group_stride_bytes,
-                           long long groups, cudaStream_t s, int sm_count)
+                           long long groups, cudaStream_t s, int sm_count, int *err)
 {
     const long long gs = group_stride_bytes / 4;
     if (wavelet == CDF97)
-        return inverse ? launch_t<4, true>(base, N, G, gs, groups, s, sm_count)
-                       : launch_t<4, false>(base, N, G, gs, groups, s, sm_count);
-    return inverse ? launch_t<2, true>(base, N, G, gs, groups, s, sm_count)
-                   : launch_t<2, false>(base, N, G, gs, groups, s, sm_count);
+        return inverse ? launch_t<4, true>(base, N, G, gs, groups, s, sm_count, err)
+                       : launch_t<4, false>(base, N, G, gs, groups, s, sm_count, err);
+    return inverse ? launch_t<2, true>(base, N, G, gs, groups, s, sm_count, err)
+                   : launch_t<2, false>(base, N, G, gs, groups, s, sm_count, err);
 }
 
 }  // namespace dwt

@@ -16,6 +16,6 @@ bool signals_fast_ok(const void *base, int N, long long stride, int G, long long
 
 // One level over `groups` groups of G signals of N samples, in place.
 cudaError_t launch_signals(int wavelet, bool inverse, float *base, int N, int G, long long group_stride_bytes,
-                           long long groups, cudaStream_t s, int sm_count);
+                           long long groups, cudaStream_t s, int sm_count, int *err);
 
 }  // namespace dwt
