@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -34,6 +35,7 @@
 #include "../../include/libdwt.h"
 #include "dwt_batch.cuh"
 #include "dwt_capi_internal.h"
+#include "dwt_coarse.cuh"
 #include "dwt_lines.cuh"
 #include "dwt_units.cuh"
 
@@ -110,7 +112,8 @@ __device__ void tail_item(const BatchImage &I, float *smem, int lane)
 {
     const int j0 = I.j_tail;
     const int w0 = ceil_div_pow2(I.w, j0), h0 = ceil_div_pow2(I.h, j0);
-    const int P = w0 + 1, PT = h0 + 1;
+    // line pitches rounded up to 4 floats: every line starts 16-byte aligned
+    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
     float *A = smem, *B = smem + P * h0;
     const Wavelet W = make_wavelet_dev(I.wavelet, I.inverse);
     const int levels = I.J - j0;
@@ -239,7 +242,7 @@ constexpr int kRingFloats = kStages * kStageFloats;
 
 bool tail_fits(int w, int h, int side)
 {
-    return side > 0 && w <= side && h <= side && (w + 1) * h + (h + 1) * w <= kRingFloats;
+    return side > 0 && w <= side && h <= side && coarse_pitch(w) * h + coarse_pitch(h) * w <= kRingFloats;
 }
 
 }  // namespace

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(kThreads)
 coarse_forward_kernel(const float *in, long long in_pitch, int w0, int h0, int levels, float *out,
                       long long out_pitch, const Wavelet W)
 {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
     float *A = sm, *B = sm + P * h0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kThreads)
 coarse_inverse_kernel(const float *in, long long in_pitch, int w0, int h0, int levels, float *out,
                       long long out_pitch, const Wavelet W)
 {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
     float *A = sm, *B = sm + P * h0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -17,6 +17,8 @@ namespace lines {
 constexpr int kV = 8;  // samples per lane: one warp holds 256 samples of a line
 constexpr unsigned kAll = 0xffffffffu;
 
+__device__ __forceinline__ bool aligned16(const float *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 // Forward lifting of one line of length n (2 <= n <= 252) held by a warp,
 // sample 8*lane + k in x[k]; samples past the end hold their mirror images.
 // Every lifting step is applied uniformly; the left neighbour of sample 0 is
@@ -82,8 +84,8 @@ __device__ __forceinline__ void pass_forward(const float *src, int ls, float *ds
         st[k] = i < n ? ((k & 1) ? nd + (i >> 1) : (i >> 1)) * dp : -1;
     }
     // lanes whose 8 samples lie inside the line read them as two 16-byte
-    // loads (line pitches are multiples of 4 floats)
-    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0);
+    // loads, when every line starts on a 16-byte boundary
+    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0) && aligned16(src);
     for (int l = warp; l < nl; l += nwarps) {
         const float *line = src + l * ls;
         float x[kV];
@@ -124,7 +126,7 @@ __device__ __forceinline__ void pass_inverse(const float *src, int ls, float *ds
     }
     // lanes whose 8 samples lie inside the line read their 4 L and 4 H
     // samples as two 16-byte loads when both halves start 16-byte aligned
-    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0) && ((nd & 3) == 0);
+    const bool vec = (kV * lane + kV <= n) && ((ls & 3) == 0) && ((nd & 3) == 0) && aligned16(src);
     for (int l = warp; l < nl; l += nwarps) {
         const float *line = src + l * ls;
         float x[kV];
