@@ -35,8 +35,7 @@
 #include "../../include/libdwt.h"
 #include "dwt_batch.cuh"
 #include "dwt_capi_internal.h"
-#include "dwt_coarse.cuh"
-#include "dwt_lines.cuh"
+#include "dwt_recur.cuh"
 #include "dwt_units.cuh"
 
 namespace dwt {
@@ -106,52 +105,30 @@ __device__ LevelDesc level_desc(const BatchImage &I, int j)
     return d;
 }
 
-// All levels from j_tail on in one warp, the band in the warp's ring.
+struct WarpSync {
+    __device__ void operator()() const { __syncwarp(); }
+};
+
+// All levels from j_tail on in one warp, the band and its half-transformed
+// copy in the warp's ring (row-major, odd pitch).
 template <int NS>
 __device__ void tail_item(const BatchImage &I, float *smem, int lane)
 {
     const int j0 = I.j_tail;
     const int w0 = ceil_div_pow2(I.w, j0), h0 = ceil_div_pow2(I.h, j0);
-    // line pitches rounded up to 4 floats: every line starts 16-byte aligned
-    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
+    const int P = recur::band_pitch(w0);
     float *A = smem, *B = smem + P * h0;
     const Wavelet W = make_wavelet_dev(I.wavelet, I.inverse);
     const int levels = I.J - j0;
+    const float *in = I.inverse ? I.src : (j0 == 0 ? I.src : I.ll[(j0 - 1) & 1]);
+    const long long ip = I.inverse ? I.src_pitch : (j0 == 0 ? I.src_pitch : I.llp[(j0 - 1) & 1]);
+    for (int y = 0; y < h0; ++y)
+        for (int x = lane; x < w0; x += 32) A[y * P + x] = in[y * ip + x];
+    __syncwarp();
     if (!I.inverse) {
-        const float *in = j0 == 0 ? I.src : I.ll[(j0 - 1) & 1];
-        const long long ip = j0 == 0 ? I.src_pitch : I.llp[(j0 - 1) & 1];
-        for (int y = 0; y < h0; ++y)
-            for (int x = lane; x < w0; x += 32) A[y * P + x] = in[y * ip + x];
-        __syncwarp();
-        int w = w0, h = h0;
-        for (int lvl = 0; lvl < levels; ++lvl) {
-            const int wd = (w + 1) >> 1, hd = (h + 1) >> 1;
-            lines::pass_forward<NS>(A, P, B, PT, h, w, W, 0, 1, lane);
-            __syncwarp();
-            lines::pass_forward<NS>(B, PT, A, P, w, h, W, 0, 1, lane);
-            __syncwarp();
-            for (int y = 0; y < h; ++y)
-                for (int x = (y < hd ? wd : 0) + lane; x < w; x += 32) I.dst[y * I.dst_pitch + x] = A[y * P + x];
-            w = wd;
-            h = hd;
-        }
-        for (int y = 0; y < h; ++y)
-            for (int x = lane; x < w; x += 32) I.dst[y * I.dst_pitch + x] = A[y * P + x];
+        recur::band_forward<NS>(A, B, w0, h0, levels, I.dst, I.dst_pitch, W, lane, 32, WarpSync{});
     } else {
-        for (int y = 0; y < h0; ++y)
-            for (int x = lane; x < w0; x += 32) A[y * P + x] = I.src[y * I.src_pitch + x];
-        __syncwarp();
-        for (int lvl = levels - 1; lvl >= 0; --lvl) {
-            int w = w0, h = h0;
-            for (int k = 0; k < lvl; ++k) {
-                w = (w + 1) >> 1;
-                h = (h + 1) >> 1;
-            }
-            lines::pass_inverse<NS>(A, P, B, PT, h, w, W, 0, 1, lane);
-            __syncwarp();
-            lines::pass_inverse<NS>(B, PT, A, P, w, h, W, 0, 1, lane);
-            __syncwarp();
-        }
+        recur::band_inverse<NS>(A, B, w0, h0, levels, W, lane, 32, WarpSync{});
         float *out = j0 == 0 ? I.dst : I.ll[(j0 - 1) & 1];
         const long long op = j0 == 0 ? I.dst_pitch : I.llp[(j0 - 1) & 1];
         for (int y = 0; y < h0; ++y)
@@ -242,7 +219,7 @@ constexpr int kRingFloats = kStages * kStageFloats;
 
 bool tail_fits(int w, int h, int side)
 {
-    return side > 0 && w <= side && h <= side && coarse_pitch(w) * h + coarse_pitch(h) * w <= kRingFloats;
+    return side > 0 && w <= side && h <= side && recur::band_floats(w, h) <= kRingFloats;
 }
 
 }  // namespace

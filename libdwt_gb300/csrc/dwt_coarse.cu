@@ -3,16 +3,13 @@
 // Once the LL band is small, each further level has too little work to fill
 // the GPU and a launch per level costs more than the level itself.  This
 // kernel loads the band into shared memory and runs every remaining level
-// there.  A pass gives each line (row or column) to one warp, which holds up
-// to 256 samples in registers (8 per lane, mirrored past the end of the
-// line) and runs the lifting steps with warp shuffles, the same per-sample
-// arithmetic as the reference (x + c*(l + r), symmetric extension, scaling).
-// Each pass writes its result transposed and deinterleaved into the other
-// buffer, so the column pass reads its lines as rows too.  The forward writes
-// each level's detail bands and the final LL to the output frame; the
-// inverse reads them and writes the reconstructed band.
+// there, each level as a row pass and a column pass of per-thread lifting
+// recurrences (one thread per line segment, dwt_recur.cuh) between two
+// row-major buffers with an odd pitch, so neither pass has bank conflicts
+// and nothing is transposed.  The forward writes each level's detail bands
+// and the final LL to the output frame; the inverse reads them and writes
+// the reconstructed band.
 #include "dwt_coarse.cuh"
-#include "dwt_lines.cuh"
 
 #include <algorithm>
 
@@ -21,34 +18,59 @@ namespace dwt {
 namespace {
 
 constexpr int kThreads = 1024;
-constexpr int kWarps = kThreads / 32;
-// A: the band, row-major with pitch P; B: its transpose, pitch PT.
+
+struct CtaSync {
+    __device__ void operator()() const { __syncthreads(); }
+};
+
+// Global -> shared copy of the w x h band: each thread issues kLoadBatch
+// loads before their shared-memory stores (a 128 x 128 band crosses the
+// L2 once per thread), the flat walk replayed for the stores.
+constexpr int kLoadBatch = 16;
+__device__ __forceinline__ void load_band(float *A, int P, const float *__restrict__ in, long long in_pitch, int w,
+                                          int h)
+{
+    const int dy = kThreads / w, dx = kThreads - dy * w;
+    int y = threadIdx.x / w, x = threadIdx.x - y * w;
+    auto advance = [&]() {
+        x += dx;
+        y += dy;
+        if (x >= w) {
+            x -= w;
+            ++y;
+        }
+    };
+    while (y < h) {
+        const int y0 = y, x0 = x;
+        float v[kLoadBatch];
+#pragma unroll
+        for (int k = 0; k < kLoadBatch; ++k) {
+            if (y < h) v[k] = __ldg(in + y * in_pitch + x);
+            advance();
+        }
+        y = y0;
+        x = x0;
+#pragma unroll
+        for (int k = 0; k < kLoadBatch; ++k) {
+            if (y < h) A[y * P + x] = v[k];
+            advance();
+        }
+    }
+}
+
 template <int NS>
 __global__ void __launch_bounds__(kThreads)
 coarse_forward_kernel(const float *in, long long in_pitch, int w0, int h0, int levels, float *out,
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ __align__(16) float sm[];
-    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
+    const int P = recur::band_pitch(w0);
     float *A = sm, *B = sm + P * h0;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
-        for (int x = threadIdx.x & 31; x < w0; x += 32) A[y * P + x] = in[y * in_pitch + x];
+    pdl_release();
+    pdl_wait();
+    load_band(A, P, in, in_pitch, w0, h0);
     __syncthreads();
-    int w = w0, h = h0;
-    for (int lvl = 0; lvl < levels; ++lvl) {
-        const int wd = (w + 1) >> 1, hd = (h + 1) >> 1;
-        lines::pass_forward<NS>(A, P, B, PT, h, w, W, warp, kWarps, lane);  // rows -> columns of B
-        __syncthreads();
-        lines::pass_forward<NS>(B, PT, A, P, w, h, W, warp, kWarps, lane);  // columns -> rows of A
-        __syncthreads();
-        for (int y = warp; y < h; y += kWarps)
-            for (int x = (y < hd ? wd : 0) + lane; x < w; x += 32) out[y * out_pitch + x] = A[y * P + x];
-        w = wd;
-        h = hd;
-    }
-    for (int y = warp; y < h; y += kWarps)
-        for (int x = lane; x < w; x += 32) out[y * out_pitch + x] = A[y * P + x];
+    recur::band_forward<NS>(A, B, w0, h0, levels, out, out_pitch, W, threadIdx.x, kThreads, CtaSync{});
 }
 
 template <int NS>
@@ -57,27 +79,14 @@ coarse_inverse_kernel(const float *in, long long in_pitch, int w0, int h0, int l
                       long long out_pitch, const Wavelet W)
 {
     extern __shared__ __align__(16) float sm[];
-    const int P = coarse_pitch(w0), PT = coarse_pitch(h0);
+    const int P = recur::band_pitch(w0);
     float *A = sm, *B = sm + P * h0;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int y = threadIdx.x >> 5; y < h0; y += kWarps)
-        for (int x = threadIdx.x & 31; x < w0; x += 32) A[y * P + x] = in[y * in_pitch + x];
+    pdl_release();
+    pdl_wait();
+    load_band(A, P, in, in_pitch, w0, h0);
     __syncthreads();
-    for (int lvl = levels - 1; lvl >= 0; --lvl) {
-        int w = w0, h = h0;
-        for (int k = 0; k < lvl; ++k) {
-            w = (w + 1) >> 1;
-            h = (h + 1) >> 1;
-        }
-        // rows first (src/libdwt.c:6706-6717): rows of A -> columns of B
-        lines::pass_inverse<NS>(A, P, B, PT, h, w, W, warp, kWarps, lane);
-        __syncthreads();
-        // then columns: columns of B hold the L rows then the H rows
-        lines::pass_inverse<NS>(B, PT, A, P, w, h, W, warp, kWarps, lane);
-        __syncthreads();
-    }
-    for (int y = warp; y < h0; y += kWarps)
-        for (int x = lane; x < w0; x += 32) out[y * out_pitch + x] = A[y * P + x];
+    recur::band_inverse<NS>(A, B, w0, h0, levels, W, threadIdx.x, kThreads, CtaSync{});
+    recur::copy_rect(A, P, out, out_pitch, 0, w0, 0, h0, threadIdx.x, kThreads);
 }
 
 template <typename K>
@@ -102,19 +111,22 @@ cudaError_t launch_coarse(bool inverse, const float *in, long long in_pitch, int
     }
     if (!coarse_fits(w, h)) return cudaErrorInvalidValue;
     const Wavelet W = make_wavelet(wavelet, inverse);
-    const size_t smem = size_t(4) * (coarse_pitch(w) * h + coarse_pitch(h) * w);
+    const size_t smem = size_t(4) * recur::band_floats(w, h);
     if (wavelet == CDF97) {
         if (inverse)
-            coarse_inverse_kernel<4><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+            return launch_pdl(coarse_inverse_kernel<4>, dim3(1), dim3(kThreads), smem, s, in, in_pitch, w, h, levels, out,
+                              out_pitch, W);
         else
-            coarse_forward_kernel<4><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+            return launch_pdl(coarse_forward_kernel<4>, dim3(1), dim3(kThreads), smem, s, in, in_pitch, w, h, levels, out,
+                              out_pitch, W);
     } else {
         if (inverse)
-            coarse_inverse_kernel<2><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+            return launch_pdl(coarse_inverse_kernel<2>, dim3(1), dim3(kThreads), smem, s, in, in_pitch, w, h, levels, out,
+                              out_pitch, W);
         else
-            coarse_forward_kernel<2><<<1, kThreads, smem, s>>>(in, in_pitch, w, h, levels, out, out_pitch, W);
+            return launch_pdl(coarse_forward_kernel<2>, dim3(1), dim3(kThreads), smem, s, in, in_pitch, w, h, levels, out,
+                              out_pitch, W);
     }
-    return cudaGetLastError();
 }
 
 }  // namespace dwt

@@ -2,19 +2,17 @@
 #pragma once
 
 #include "dwt_common.cuh"
+#include "dwt_recur.cuh"
 
 namespace dwt {
 
-// Shared memory of the coarse kernel: the band and its transpose, line
-// pitches rounded up to 4 floats (16-byte line starts).
+// Shared memory of the coarse kernel: the band and its half-transformed
+// copy, row-major with an odd pitch.
 constexpr int kCoarseSmem = 200 * 1024;
-__host__ __device__ inline int coarse_pitch(int n) { return (n + 3) & ~3; }
-// Bands the coarse kernel takes: lines of at most 252 samples (one warp), and
-// both buffers within kCoarseSmem.
+// Bands the coarse kernel takes: both buffers within kCoarseSmem.
 __host__ __device__ inline bool coarse_fits(int w, int h)
 {
-    return w >= 1 && h >= 1 && w <= 252 && h <= 252 &&
-           4LL * ((long long)coarse_pitch(w) * h + (long long)coarse_pitch(h) * w) <= kCoarseSmem;
+    return w >= 1 && h >= 1 && 4LL * recur::band_floats(w, h) <= kCoarseSmem;
 }
 
 // Forward: `in` is the w x h LL band entering level j0; runs `levels` levels

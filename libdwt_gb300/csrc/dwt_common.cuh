@@ -216,4 +216,33 @@ enum DeviceError : int {
     kErrQueueTimeout = 2,  // a work-queue dependency wait gave up
 };
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may be
+// scheduled while its predecessor in the stream is still draining; it calls
+// pdl_wait() before touching global memory (the wait returns once the
+// predecessor has completed and its writes are visible) and pdl_release()
+// to let its own successor start launching.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Whether level kernels are chained with programmatic dependent launch
+// (default on; DWT_GPU_PDL=0 turns it off).
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace dwt

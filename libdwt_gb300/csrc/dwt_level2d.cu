@@ -5,8 +5,18 @@
 #include "dwt_units.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 
 namespace dwt {
+
+bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_PDL");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
 Wavelet make_wavelet(int id, bool inverse)
 {
@@ -30,6 +40,8 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err)
     float *ring = units::warp_ring(smem, warp);
     uint64_t *bars = units::warp_bars(smem, warp, kWarpsPerCta);
     units::init_bars(bars, lane);
+    pdl_release();
+    pdl_wait();
     const bool fast_launch = units::fast_ok<INV>(D);
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
@@ -51,8 +63,7 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
     }
     const int units = d.n_strips * d.n_segs;
     const int grid = ceil_div(units, kWarpsPerCta);
-    level_kernel<NS, INV><<<grid, kWarpsPerCta * 32, kSmemBytes, stream>>>(d, W, err);
-    return cudaGetLastError();
+    return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, d, W, err);
 }
 
 }  // namespace

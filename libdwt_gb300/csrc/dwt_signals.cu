@@ -11,6 +11,7 @@
 // of a group's samples are read before any is written, so in place is safe,
 // and each sample crosses HBM once each way (8 bytes per sample).
 #include "dwt_signals.cuh"
+#include "dwt_recur.cuh"
 
 #include <algorithm>
 
@@ -20,85 +21,6 @@ namespace {
 
 constexpr int kSigThreads = 512;
 constexpr uint32_t kBulkChunk = 32768;  // bytes per bulk copy
-
-// Forward recurrence along one signal, output samples [k0, k1) of L (and H).
-template <int NS>
-__device__ void forward_signal(const float *x, int G, int N, float *gsig, int k0, int k1, const Wavelet &W)
-{
-    constexpr int LAT = NS / 2;
-    const int nl = (N + 1) >> 1;
-    float e = 0, o = 0, o1 = 0, e1 = 0, o2 = 0;
-    for (int m = k0 - LAT; m < k1 + LAT; ++m) {
-        int ra = 2 * m, rb = 2 * m + 1;
-        if (ra < 0 || rb >= N) {
-            ra = mirror(ra, N);
-            rb = mirror(rb, N);
-        }
-        const float A = x[ra * G], B = x[rb * G];
-        float L, H;
-        if (NS == 4) {
-            const float o1n = lift(o, W.c[0], e, A);
-            const float e1n = lift(e, W.c[1], o1, o1n);
-            const float o2n = lift(o1, W.c[2], e1, e1n);
-            const float e2n = lift(e1, W.c[3], o2, o2n);
-            L = fmul(e2n, W.zeta_e);
-            H = fmul(o2n, W.zeta_o);
-            o1 = o1n; e1 = e1n; o2 = o2n;
-        } else {
-            const float o1n = lift(o, W.c[0], e, A);
-            const float e1n = lift(e, W.c[1], o1, o1n);
-            L = fmul(e1n, W.zeta_e);
-            H = fmul(o1n, W.zeta_o);
-            o1 = o1n;
-        }
-        e = A;
-        o = B;
-        const int p = m - LAT;
-        if (p >= k0) {
-            gsig[p * G] = L;
-            if (2 * p + 1 < N) gsig[(nl + p) * G] = H;
-        }
-    }
-}
-
-template <int NS>
-__device__ void inverse_signal(const float *x, int G, int N, float *gsig, int k0, int k1, const Wavelet &W)
-{
-    constexpr int LAT = NS / 2;
-    const int nl = (N + 1) >> 1;
-    float o = 0, e1 = 0, o1 = 0, e2 = 0;
-    for (int m = k0 - LAT; m < k1 + LAT; ++m) {
-        int ra = 2 * m, rb = 2 * m + 1;
-        if (ra < 0 || rb >= N) {
-            ra = mirror(ra, N);
-            rb = mirror(rb, N);
-        }
-        const float E = fmul(x[(ra >> 1) * G], W.zeta_o);
-        const float O = fmul(x[(nl + (rb >> 1)) * G], W.zeta_e);
-        float Ev, Ov;
-        if (NS == 4) {
-            const float e1n = lift(E, W.c[0], o, O);
-            const float o1n = lift(o, W.c[1], e1, e1n);
-            const float e2n = lift(e1, W.c[2], o1, o1n);
-            const float o2n = lift(o1, W.c[3], e2, e2n);
-            Ev = e2;
-            Ov = o2n;
-            e1 = e1n; o1 = o1n; e2 = e2n;
-        } else {
-            const float e1n = lift(E, W.c[0], o, O);
-            const float o1n = lift(o, W.c[1], e1, e1n);
-            Ev = e1;
-            Ov = o1n;
-            e1 = e1n;
-        }
-        o = O;
-        const int p = m - LAT;
-        if (p >= k0) {
-            gsig[(2 * p) * G] = Ev;
-            if (2 * p + 1 < N) gsig[(2 * p + 1) * G] = Ov;
-        }
-    }
-}
 
 template <int NS, bool INV>
 __global__ void __launch_bounds__(kSigThreads)
@@ -139,9 +61,9 @@ signals_kernel(float *base, int N, int G, long long group_stride_f, long long gr
             for (int k0 = c * seg; k0 < npairs; k0 += per_signal * seg) {
                 const int k1 = min(k0 + seg, npairs);
                 if (INV)
-                    inverse_signal<NS>(sx + s, G, N, gb + s, k0, k1, W);
+                    recur::line_inverse<NS>(sx + s, G, N, gb + s, G, k0, k1, W);
                 else
-                    forward_signal<NS>(sx + s, G, N, gb + s, k0, k1, W);
+                    recur::line_forward<NS>(sx + s, G, N, gb + s, G, k0, k1, W);
             }
         }
         __syncthreads();  // every thread is done with the staged block
