@@ -254,7 +254,7 @@ static cudaError_t dense_forward_levels(const float *in, long long in_pitch, flo
     const int j0 = std::max(coarse_level(W, H, J), j_begin);
     for (int j = j_begin; j < j0; ++j) {
         LevelDesc d = fwd_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
-        plan_level(d, seg_hint);
+        plan_level(d, seg_hint, false);
         cudaError_t e = launch_level(d, wavelet, false, s, err);
         if (e != cudaSuccess) return e;
     }
@@ -287,7 +287,7 @@ static cudaError_t dense_inverse_levels(const float *in, long long in_pitch, flo
     }
     for (int j = jtop; j >= j_end; --j) {
         LevelDesc d = inv_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
-        plan_level(d, seg_hint);
+        plan_level(d, seg_hint, true);
         cudaError_t e = launch_level(d, wavelet, true, s, err);
         if (e != cudaSuccess) return e;
     }
@@ -349,7 +349,7 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     const int LAT = wavelet == CDF97 ? 2 : 1;
     const int wd = (W + 1) / 2, hd = (H + 1) / 2, hh = H / 2;
     LevelDesc d0 = fwd_desc(in.f(), P, out.f(), P, W, H, J, 0, buf, p);
-    plan_level(d0, 0);
+    plan_level(d0, 0, false);
     const int npairs = (H + 1) / 2, seg = d0.seg_pairs, nsegs = d0.n_segs;
     const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
     std::vector<HostOut> pending;
@@ -431,7 +431,7 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
     if (J > 1) CK(dense_inverse_levels(in.f(), P, out.f(), P, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
 
     LevelDesc d1 = inv_desc(in.f(), P, out.f(), P, W, H, J, 1, buf, p);
-    plan_level(d1, 0);
+    plan_level(d1, 0, true);
     const int npairs = (H + 1) / 2, seg = d1.seg_pairs, nsegs = d1.n_segs;
     const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
     int top_in = 0, bot_in = 0, b = 1;
@@ -690,7 +690,7 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
         d.out[0] = out.f();
         d.out_pitch[0] = P;
     }
-    plan_level(d, 0);
+    plan_level(d, 0, inverse);
     CK(launch_level(d, wavelet, inverse, s, c.d_err));
     if (!inverse) {
         CK(scatter(out.f(), c_l, nl));
@@ -778,7 +778,7 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
         d.out[0] = out.f();
         d.out_pitch[0] = P;
     }
-    plan_level(d, 0);
+    plan_level(d, 0, inverse);
     CK(launch_level(d, wavelet, inverse, s, c.d_err));
     void *dst = on_device ? base : span.p;
     CK(launch_scatter_signals(out.f(), P, N, dst, stride, count, group, group_stride, lane_stride, s));
@@ -914,7 +914,7 @@ int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const float *const
         d.out[k] = out[k];
         d.out_pitch[k] = out_pitch_bytes[k] / 4;
     }
-    plan_level(d, 0);
+    plan_level(d, 0, inverse != 0);
     Context &c = ctx();
     cudaError_t e = launch_level(d, wavelet, inverse != 0, static_cast<cudaStream_t>(stream), c.d_err);
     if (e != cudaSuccess) {

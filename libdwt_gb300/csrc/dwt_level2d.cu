@@ -68,20 +68,48 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
 
 }  // namespace
 
-void plan_level(LevelDesc &d, int seg_pairs_hint)
+namespace {
+
+// Segment length of a 2D level, measured on the levels of 16384^2 (level
+// kernel times under ncu): the forward is fastest with about 176 segments
+// per level (none shorter than 8 pairs from 1024 row pairs up, 4 below);
+// the inverse with about 88 on large levels and 128 (at least 4 pairs) from
+// 1024 row pairs down.
+constexpr int kSegsForward = 176;
+constexpr int kSegsInverse = 88;
+constexpr int kSegsInverseSmall = 128;
+constexpr int kSmallPairs = 1024;
+
+int env_int(const char *name, int dflt)
+{
+    const char *v = getenv(name);
+    return (v && *v) ? atoi(v) : dflt;
+}
+
+}  // namespace
+
+void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
 {
     const bool one_row = (d.h == 1) || d.rows_only;
     const int npairs = one_row ? d.h : (d.h + 1) / 2;
     d.n_strips = ceil_div(d.w, kStripOut);
     int seg = seg_pairs_hint;
     if (seg <= 0) {
-        // About 1.5 units per resident warp (152 SMs x 24 warps): long
-        // segments on large levels keep the 2*LAT warm-up pairs a few percent
-        // of the work; small levels get short segments for parallelism.
-        const long long target_units = 152LL * 24 * 3 / 2;
-        seg = int(((long long)npairs * d.n_strips + target_units - 1) / target_units);
-        seg = std::max(seg, one_row ? 1 : 4);
-        seg = std::min(seg, 256);
+        if (one_row) {
+            // rows are independent: about 1.5 units per resident warp
+            const long long target_units = 152LL * 20 * 3 / 2;
+            seg = int(std::max(1LL, ((long long)npairs * d.n_strips + target_units - 1) / target_units));
+            seg = std::min(seg, 256);
+        } else {
+            static const int segs_f = std::max(1, env_int("DWT_GPU_SEGS_FWD", kSegsForward));
+            static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
+            if (!inverse)
+                seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : 4);
+            else if (npairs > kSmallPairs)
+                seg = std::max(ceil_div(npairs, segs_i), 4);
+            else
+                seg = std::max(ceil_div(npairs, kSegsInverseSmall), 4);
+        }
     }
     seg = std::min(seg, std::max(npairs, 1));
     d.seg_pairs = seg;

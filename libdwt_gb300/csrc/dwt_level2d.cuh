@@ -40,8 +40,9 @@ struct LevelDesc {
     long long out_pitch[4];
 };
 
-// Fills n_strips / seg_pairs / n_segs for a level of size w x h.
-void plan_level(LevelDesc &d, int seg_pairs_hint);
+// Fills n_strips / seg_pairs / n_segs for a level of size w x h (the
+// segment length depends on the direction).
+void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse);
 
 // Launch one level on `stream`.  err: device error word (may be null).
 cudaError_t launch_level(const LevelDesc &d, int wavelet, bool inverse, cudaStream_t stream,

@@ -272,60 +272,100 @@ __device__ __forceinline__ void v_forward2(f2 A, f2 B, f2 &e, f2 &o, f2 &o1, f2 
     o = B;
 }
 
+// ------------------------------------------------------------ staging pipes
+//
+// A 2D unit streams `iters` stages (two row pairs each) through a ring of
+// shared-memory slots; the pipe owns the slots and their barriers, the unit
+// says what a stage holds.  Iterations are numbered by a running tick, so a
+// ring carries on across the units a warp takes in turn.
+//
+// WarpPipe: a warp's private ring.  Its lane 0 issues every stage and
+// refills a slot as soon as the warp has read it (the warp's own program
+// order orders the reuse).
+struct WarpPipe {
+    float *ring;
+    uint64_t *full;
+    static constexpr int kDepth = kStages;
+    static constexpr int kLag = 0;  // after reading iteration u, issue u + kDepth - kLag
+    __device__ __forceinline__ float *slot(uint32_t t) const { return ring + (t % kDepth) * kStageFloats; }
+    __device__ __forceinline__ uint64_t *bar(uint32_t t) const { return &full[t % kDepth]; }
+    __device__ __forceinline__ bool wait(uint32_t t) const
+    {
+        return mbar_wait_bounded(&full[t % kDepth], (t / kDepth) & 1u);
+    }
+    __device__ __forceinline__ bool producer(int lane) const { return lane == 0; }
+    __device__ __forceinline__ bool acquire(uint32_t) const { return true; }
+    __device__ __forceinline__ void release(uint32_t, int) const { __syncwarp(); }
+};
+
+// Stage count of a 2D unit of segment `seg`: pairs k0-LAT .. k1+LAT-1, two
+// per stage.
+template <int NS>
+__device__ __forceinline__ void unit_span(const LevelDesc &D, int seg, int &k0, int &total, int &iters)
+{
+    constexpr int LAT = NS / 2;
+    const int npairs = (D.h + 1) >> 1;
+    k0 = seg * D.seg_pairs;
+    const int k1 = min(k0 + D.seg_pairs, npairs);
+    total = k1 - k0 + 2 * LAT;
+    iters = (total + 1) >> 1;
+}
+
 // One unit of the fused forward level: interleaved rows in, four bands out.
 // Per row pair m (rows 2m, 2m+1, mirrored at the borders) the vertical
 // recurrence emits output pair m - LAT; pairs k0-LAT .. k1+LAT-1 are walked
 // so that the unit's outputs k0 .. k1-1 are exact.  EDGE selects the general
 // path for strips touching the left or right border (mirrored columns,
-// partial lanes) or unaligned outputs.
-template <int NS, bool EDGE>
-__device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                             uint64_t *bars, uint32_t &tick, int lane, int *err)
+// partial lanes) or unaligned outputs.  The rows are staged from column B
+// on, `win` columns wide, `slot_f` floats per row slot.
+template <int NS, bool EDGE, class Pipe>
+__device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
+                             int win, int slot_f, uint32_t &tick, int lane, int *err)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
     const int b = strip * kStripOut - 4;  // interleaved column held by lane 0, value 0
-    const int npairs = (h + 1) >> 1;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, npairs);
+    int k0, total, iters;
+    unit_span<NS>(D, seg, k0, total, iters);
     const int m0 = k0 - LAT;
-    const int total = k1 - k0 + 2 * LAT;  // row pairs walked
-    const int iters = (total + 1) >> 1;   // two pairs per stage
 
     // staged column window [lo, hi) of every row
     const int w4 = (w + 3) & ~3;
-    const int lo = max(b, 0), hi = min(b + kStripIn, w4);
+    const int lo = max(B, 0), hi = min(B + win, w4);
     const uint32_t bytes = uint32_t(hi - lo) * 4u;
-    const int dst_off = lo - b;
+    const int dst_off = lo - B;
     const float *srow = D.in[0] + lo;
     const long long pitch = D.in_pitch[0];
 
-    // this lane's shared-memory offsets (mirrored at the borders)
+    // this lane's slot offsets (mirrored at the borders)
     int off[4];
     if (EDGE) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) off[i] = min(max(mirror(b + 4 * lane + i, w) - b, lo - b), hi - b - 1);
+        for (int i = 0; i < 4; ++i) off[i] = min(max(mirror(b + 4 * lane + i, w) - B, lo - B), hi - B - 1);
     } else {
-        off[0] = 4 * lane;
+        off[0] = b - B + 4 * lane;
     }
 
-    if (lane == 0) {
+    const uint32_t t0 = tick;
+    bool issued_ok = true;
+    auto issue = [&](int u) {
+        const uint32_t t = t0 + u;
+        if (!pipe.acquire(t)) return false;
+        float *dst = pipe.slot(t) + dst_off;
+        uint64_t *bar = pipe.bar(t);
         fence_proxy_async_smem();
-        Cursor pc = cursor_at(tick);
-        const int n0 = min(iters, kStages);
-        for (int u = 0; u < n0; ++u) {
-            float *slot = ring + pc.st * kStageFloats + dst_off;
-            mbar_arrive_expect_tx(&bars[pc.st], 4 * bytes);
+        mbar_arrive_expect_tx(bar, 4 * bytes);
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * u + r, h, ra, rb);
-                bulk_g2s(slot + (2 * r) * kSlotF, srow + ra * pitch, bytes, &bars[pc.st]);
-                bulk_g2s(slot + (2 * r + 1) * kSlotF, srow + rb * pitch, bytes, &bars[pc.st]);
-            }
-            pc.next();
+        for (int r = 0; r < 2; ++r) {
+            int ra, rb;
+            pair_rows(m0 + 2 * u + r, h, ra, rb);
+            bulk_g2s(dst + (2 * r) * slot_f, srow + ra * pitch, bytes, bar);
+            bulk_g2s(dst + (2 * r + 1) * slot_f, srow + rb * pitch, bytes, bar);
         }
-    }
+        return true;
+    };
+    if (pipe.producer(lane))
+        for (int u = 0; u < min(iters, Pipe::kDepth) && issued_ok; ++u) issued_ok = issue(u);
     __syncwarp();
 
     // packed constants
@@ -349,19 +389,18 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
 
     f2 e[2] = {0, 0}, o[2] = {0, 0}, o1[2] = {0, 0}, e1[2] = {0, 0}, o2[2] = {0, 0};
 
-    Cursor c = cursor_at(tick);
     int t = 0;  // pair counter
 #pragma unroll 1
     for (int u = 0; u < iters; ++u) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
+        if (!__all_sync(kFull, pipe.wait(t0 + u))) {
             if (lane == 0) raise_error(err, kErrWaitTimeout);
             return false;
         }
-        const float *slot = ring + c.st * kStageFloats;
+        const float *slot = pipe.slot(t0 + u);
         f2 E[4], O[4];  // rows 0..3 of the stage
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            const float *row = slot + r * kSlotF;
+            const float *row = slot + r * slot_f;
             if (EDGE) {
                 E[r] = pk(row[off[0]], row[off[2]]);
                 O[r] = pk(row[off[1]], row[off[3]]);
@@ -371,6 +410,10 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                 O[r] = pk(v.y, v.w);
             }
         }
+        // the stage is read: release it, and issue the one kDepth - kLag ahead
+        pipe.release(t0 + u, lane);
+        if (pipe.producer(lane) && issued_ok && u >= Pipe::kLag && u - Pipe::kLag + Pipe::kDepth < iters)
+            issued_ok = issue(u - Pipe::kLag + Pipe::kDepth);
         // rows: horizontal lifting (a single-sample row is only scaled)
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -380,20 +423,6 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                 h_forward2<NS>(E[r], O[r], C, ZE, ZO);
             }
         }
-        // the stage is consumed: refill it with the pairs kStages stages ahead
-        __syncwarp();
-        if (lane == 0 && u + kStages < iters) {
-            float *dst = ring + c.st * kStageFloats + dst_off;
-            mbar_arrive_expect_tx(&bars[c.st], 4 * bytes);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * (u + kStages) + r, h, ra, rb);
-                bulk_g2s(dst + (2 * r) * kSlotF, srow + ra * pitch, bytes, &bars[c.st]);
-                bulk_g2s(dst + (2 * r + 1) * kSlotF, srow + rb * pitch, bytes, &bars[c.st]);
-            }
-        }
-        c.next();
 
         // columns: two steps of the vertical recurrence (two row pairs)
 #pragma unroll
@@ -429,8 +458,12 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
             }
         }
     }
+    // a failed issue (the producer gave up waiting for a slot) fails the
+    // whole warp, uniformly
+    const bool ok = __all_sync(kFull, issued_ok);
+    if (!ok && lane == 0) raise_error(err, kErrWaitTimeout);
     tick += iters;
-    return true;
+    return ok;
 }
 
 // ------------------------------------------------------------------ inverse
@@ -572,27 +605,27 @@ __device__ __forceinline__ void v_inverse2(f2 A, f2 B, f2 &o, f2 &e1, f2 &o1, f2
 // Per pair m the stage holds the LL and HL rows of L-row ra/2 and the LH and
 // HH rows of H-row rb/2 (ra, rb the mirrored interleaved rows 2m, 2m+1); the
 // horizontal inverse rebuilds both interleaved rows, the vertical recurrence
-// emits output rows 2(m-LAT), 2(m-LAT)+1.
-template <int NS, bool EDGE>
-__device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                             uint64_t *bars, uint32_t &tick, int lane, int *err)
+// emits output rows 2(m-LAT), 2(m-LAT)+1.  The band rows are staged from
+// band column B/2 on, `band_win` columns wide, `slot_i` floats per band-row
+// slot.
+template <int NS, bool EDGE, class Pipe>
+__device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
+                             int band_win, int slot_i, uint32_t &tick, int lane, int *err)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
     const int b = strip * kStripOut - 4;
     const int bq = b >> 1;  // band column of lane 0's first value
+    const int bqB = B >> 1;  // band column of the staged window's start
     const int Lw = (w + 1) >> 1, Hw = w >> 1;
-    const int npairs = (h + 1) >> 1;
-    const int k0 = seg * D.seg_pairs;
-    const int k1 = min(k0 + D.seg_pairs, npairs);
+    int k0, total, iters;
+    unit_span<NS>(D, seg, k0, total, iters);
     const int m0 = k0 - LAT;
-    const int total = k1 - k0 + 2 * LAT;
-    const int iters = (total + 1) >> 1;
 
     // staged band column windows; the shift is the same for every row
     // because source pitches are multiples of 4 floats
-    const int loL = max(bq, 0), hiL = min(bq + 64, Lw);
-    const int loH = loL, hiH = min(bq + 64, Hw);
+    const int loL = max(bqB, 0), hiL = min(bqB + band_win, Lw);
+    const int loH = loL, hiH = min(bqB + band_win, Hw);
     BandIn iLL, iHL, iLH, iHH;
     iLL.init(D.in[0], D.in_pitch[0], loL, hiL - loL);
     iHL.init(D.in[1], D.in_pitch[1], loH, hiH - loH);
@@ -615,39 +648,43 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
             const int lo_k = k ? loH : loL;
             const int oa = bi - lo_k + (k ? iHL.shift : iLL.shift);
             const int ob = bi - lo_k + (k ? iHH.shift : iLH.shift);
-            offA[i] = k * kSlotI + min(max(oa, 0), kSlotI - 1);
-            offB[i] = (2 + k) * kSlotI + min(max(ob, 0), kSlotI - 1);
+            offA[i] = k * slot_i + min(max(oa, 0), slot_i - 1);
+            offB[i] = (2 + k) * slot_i + min(max(ob, 0), slot_i - 1);
         }
     } else {
-        offA[0] = 2 * lane + iLL.shift;
-        offA[1] = kSlotI + 2 * lane + iHL.shift;
-        offB[0] = 2 * kSlotI + 2 * lane + iLH.shift;
-        offB[1] = 3 * kSlotI + 2 * lane + iHH.shift;
+        const int d = bq - loL + 2 * lane;
+        offA[0] = d + iLL.shift;
+        offA[1] = slot_i + d + iHL.shift;
+        offB[0] = 2 * slot_i + d + iLH.shift;
+        offB[1] = 3 * slot_i + d + iHH.shift;
     }
 
-    if (lane == 0) {
+    const uint32_t t0 = tick;
+    bool issued_ok = true;
+    auto issue = [&](int u) {
+        const uint32_t t = t0 + u;
+        if (!pipe.acquire(t)) return false;
+        float *slot = pipe.slot(t);
+        uint64_t *bar = pipe.bar(t);
         fence_proxy_async_smem();
-        Cursor pc = cursor_at(tick);
-        const int n0 = min(iters, kStages);
-        for (int u = 0; u < n0; ++u) {
-            float *slot = ring + pc.st * kStageFloats;
-            mbar_arrive_expect_tx(&bars[pc.st], tx);
+        mbar_arrive_expect_tx(bar, tx);
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * u + r, h, ra, rb);
-                const int qa = ra >> 1, qb = rb >> 1;
-                float *sl = slot + 4 * r * kSlotI;
-                bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, &bars[pc.st]);
-                bulk_g2s(sl + 2 * kSlotI, iLH.base + qb * iLH.pitch, iLH.bytes, &bars[pc.st]);
-                if (iHL.bytes) {
-                    bulk_g2s(sl + kSlotI, iHL.base + qa * iHL.pitch, iHL.bytes, &bars[pc.st]);
-                    bulk_g2s(sl + 3 * kSlotI, iHH.base + qb * iHH.pitch, iHH.bytes, &bars[pc.st]);
-                }
+        for (int r = 0; r < 2; ++r) {
+            int ra, rb;
+            pair_rows(m0 + 2 * u + r, h, ra, rb);
+            const int qa = ra >> 1, qb = rb >> 1;
+            float *sl = slot + 4 * r * slot_i;
+            bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, bar);
+            bulk_g2s(sl + 2 * slot_i, iLH.base + qb * iLH.pitch, iLH.bytes, bar);
+            if (iHL.bytes) {
+                bulk_g2s(sl + slot_i, iHL.base + qa * iHL.pitch, iHL.bytes, bar);
+                bulk_g2s(sl + 3 * slot_i, iHH.base + qb * iHH.pitch, iHH.bytes, bar);
             }
-            pc.next();
         }
-    }
+        return true;
+    };
+    if (pipe.producer(lane))
+        for (int u = 0; u < min(iters, Pipe::kDepth) && issued_ok; ++u) issued_ok = issue(u);
     __syncwarp();
 
     f2 C[4];
@@ -667,19 +704,18 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
 
     f2 o[2] = {0, 0}, e1[2] = {0, 0}, o1[2] = {0, 0}, e2[2] = {0, 0};
 
-    Cursor c = cursor_at(tick);
     int t = 0;
 #pragma unroll 1
     for (int u = 0; u < iters; ++u) {
-        if (!mbar_wait_bounded(&bars[c.st], c.par)) {
+        if (!__all_sync(kFull, pipe.wait(t0 + u))) {
             if (lane == 0) raise_error(err, kErrWaitTimeout);
             return false;
         }
-        const float *slot = ring + c.st * kStageFloats;
+        const float *slot = pipe.slot(t0 + u);
         f2 E[4], O[4];  // interleaved rows: pair 0 L-row, H-row, pair 1 L-row, H-row
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-            const float *sl = slot + 4 * r * kSlotI;
+            const float *sl = slot + 4 * r * slot_i;
             if (EDGE) {
                 E[2 * r] = pk(sl[offA[0]], sl[offA[2]]);
                 O[2 * r] = pk(sl[offA[1]], sl[offA[3]]);
@@ -692,6 +728,9 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                 O[2 * r + 1] = *reinterpret_cast<const f2 *>(sl + offB[1]);
             }
         }
+        pipe.release(t0 + u, lane);
+        if (pipe.producer(lane) && issued_ok && u >= Pipe::kLag && u - Pipe::kLag + Pipe::kDepth < iters)
+            issued_ok = issue(u - Pipe::kLag + Pipe::kDepth);
         // rows first (src/libdwt.c:6706-6717), then columns
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -701,25 +740,6 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                 h_inverse2<NS>(E[r], O[r], C, ZE, ZO);
             }
         }
-        __syncwarp();
-        if (lane == 0 && u + kStages < iters) {
-            float *slot2 = ring + c.st * kStageFloats;
-            mbar_arrive_expect_tx(&bars[c.st], tx);
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                int ra, rb;
-                pair_rows(m0 + 2 * (u + kStages) + r, h, ra, rb);
-                const int qa = ra >> 1, qb = rb >> 1;
-                float *sl = slot2 + 4 * r * kSlotI;
-                bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, &bars[c.st]);
-                bulk_g2s(sl + 2 * kSlotI, iLH.base + qb * iLH.pitch, iLH.bytes, &bars[c.st]);
-                if (iHL.bytes) {
-                    bulk_g2s(sl + kSlotI, iHL.base + qa * iHL.pitch, iHL.bytes, &bars[c.st]);
-                    bulk_g2s(sl + 3 * kSlotI, iHH.base + qb * iHH.pitch, iHH.bytes, &bars[c.st]);
-                }
-            }
-        }
-        c.next();
 
 #pragma unroll
         for (int r = 0; r < 2; ++r, ++t) {
@@ -745,10 +765,11 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
             }
         }
     }
+    const bool okw = __all_sync(kFull, issued_ok);
+    if (!okw && lane == 0) raise_error(err, kErrWaitTimeout);
     tick += iters;
-    return true;
+    return okw;
 }
-
 
 // Whether interior units of a launch may use vector loads and stores: every
 // band pointer and pitch must keep them aligned.
@@ -771,7 +792,8 @@ __device__ __forceinline__ bool fast_ok(const LevelDesc &D)
     return ok;
 }
 
-// Runs one unit (strip, seg) of the level described by D.
+// Runs one unit (strip, seg) of the level described by D on a warp's
+// private ring.
 template <int NS, bool INV>
 __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
                                          uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch)
@@ -781,11 +803,12 @@ __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, i
                    : forward_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err);
     const int b = strip * kStripOut - 4;
     const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
+    const WarpPipe pipe{ring, bars};
     if (INV)
-        return edge ? inverse_unit<NS, true>(D, W, strip, seg, ring, bars, tick, lane, err)
-                    : inverse_unit<NS, false>(D, W, strip, seg, ring, bars, tick, lane, err);
-    return edge ? forward_unit<NS, true>(D, W, strip, seg, ring, bars, tick, lane, err)
-                : forward_unit<NS, false>(D, W, strip, seg, ring, bars, tick, lane, err);
+        return edge ? inverse_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn / 2, kSlotI, tick, lane, err)
+                    : inverse_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn / 2, kSlotI, tick, lane, err);
+    return edge ? forward_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err)
+                : forward_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err);
 }
 
 // Per-warp ring and barriers inside a CTA's dynamic shared memory.
