@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace dwt {
@@ -203,6 +204,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     for (uint32_t i = 0; i < kWaitLimit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+
+// TMA tensor copy of one 2D box (the map's box shape) at element coordinates
+// (x, y) to shared memory; completion signalled on `bar` as bytes.  `dst`
+// must be 128-byte aligned and x * 4 bytes a multiple of 16.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
 }
 
 // TMA bulk copy global -> shared, completion signalled on `bar` as bytes.

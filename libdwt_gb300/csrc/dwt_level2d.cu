@@ -4,10 +4,24 @@
 #include "dwt_level2d.cuh"
 #include "dwt_units.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 namespace dwt {
+
+// Box copies for the inverse levels (default on; DWT_GPU_TMAP=0 turns them
+// off).
+bool tensor_copies_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_TMAP");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
 bool pdl_enabled()
 {
@@ -33,7 +47,7 @@ namespace {
 
 template <int NS, bool INV>
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
-level_kernel(const LevelDesc D, const Wavelet W, int *err)
+level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant__ LevelMaps M)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -43,12 +57,62 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err)
     pdl_release();
     pdl_wait();
     const bool fast_launch = units::fast_ok<INV>(D);
+    // tensor copies need 128-byte aligned slots
+    const bool maps = INV && D.tmap && (smem_addr(smem) & 127) == 0;
+    const CUtensorMap *mll = maps ? &M.ll : nullptr, *mfr = maps ? &M.frame : nullptr;
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
     for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
         const int strip = u % D.n_strips, seg = D.seg_base + u / D.n_strips;
-        if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch)) break;
+        if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr))
+            break;
     }
+}
+
+// The driver's tensor-map encoder (resolved once through the runtime).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// A w x h float region at `base` (pitch in floats) with boxes of
+// kBandRowF x 2; false if the geometry does not qualify (16-byte aligned base
+// and pitch).
+bool encode_band_map(CUtensorMap *m, const float *base, long long w, long long h, long long pitch)
+{
+    const auto enc = tensor_map_encoder();
+    if (!enc || !base || w <= 0 || h <= 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0 || (pitch & 3) != 0)
+        return false;
+    cuuint64_t dims[2] = {cuuint64_t(w), cuuint64_t(h)};
+    cuuint64_t strides[1] = {cuuint64_t(pitch) * 4};
+    cuuint32_t box[2] = {cuuint32_t(kBandRowF), 2};
+    cuuint32_t es[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of an inverse level: LL from in[0], and the frame the other
+// three bands live in (HL at +ws, LH at +hs rows, HH at both), when the
+// bands sit in one frame as the level pipeline lays them out.
+bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M)
+{
+    if (d.rows_only || d.h < 2 || d.w < 2) return false;
+    const long long ws = (d.w + 1) / 2, hs = (d.h + 1) / 2, p = d.in_pitch[2];
+    if (d.in_pitch[1] != p || d.in_pitch[3] != p) return false;
+    const float *frame = d.in[2] - hs * p;
+    if (d.in[1] != frame + ws || d.in[3] != frame + hs * p + ws) return false;
+    return encode_band_map(&M.ll, d.in[0], ws, hs, d.in_pitch[0]) && encode_band_map(&M.frame, frame, d.w, d.h, p);
 }
 
 template <int NS, bool INV>
@@ -63,7 +127,12 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
     }
     const int units = d.n_strips * d.n_segs;
     const int grid = ceil_div(units, kWarpsPerCta);
-    return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, d, W, err);
+    LevelMaps M;
+    memset(&M, 0, sizeof(M));
+    LevelDesc dd = d;
+    dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M)) ? 1 : 0;
+    return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W, err,
+                      M);
 }
 
 }  // namespace

@@ -17,8 +17,14 @@ constexpr int kLanes = 32;
 constexpr int kStripIn = 128;
 constexpr int kStripOut = 120;
 constexpr int kSlotF = 136;        // floats per forward row slot
-constexpr int kSlotI = 68;         // floats per inverse band-row slot
-constexpr int kStageFloats = 544;  // one pipeline stage = 2 row pairs: 4 rows or 8 band rows
+constexpr int kSlotI = 68;         // floats per band-row slot of the single-row units
+// Inverse 2D stages: per band (LL, HL, LH, HH) a slot of the stage's two
+// band rows, kBandRowF floats each, band slots kBandSlotF floats apart so
+// that every slot starts on a 128-byte boundary (the destination of a
+// tensor copy of a 68 x 2 box).
+constexpr int kBandRowF = 68;
+constexpr int kBandSlotF = 160;
+constexpr int kStageFloats = 640;  // one pipeline stage = 2 row pairs: 4 rows or 4 band slots
 constexpr int kStages = 4;         // pipeline depth per warp (8 row pairs)
 constexpr int kWarpsPerCta = 4;
 constexpr int kSmemBytes = kWarpsPerCta * (kStages * kStageFloats * 4 + kStages * 8);
@@ -34,10 +40,18 @@ struct LevelDesc {
     int n_strips, seg_pairs, n_segs;
     int seg_base;  // first segment of this launch (a launch may cover a sub-range)
     int rows_only;
+    int tmap;      // inverse: the tensor maps of the launch are valid (set by launch_level)
     const float *in[4];
     long long in_pitch[4];
     float *out[4];
     long long out_pitch[4];
+};
+
+// Tensor maps of an inverse level: the LL band (box kBandRowF x 2) and the
+// coefficient frame holding HL, LH, HH (the level's w x h region, same box).
+struct LevelMaps {
+    CUtensorMap ll;
+    CUtensorMap frame;
 };
 
 // Fills n_strips / seg_pairs / n_segs for a level of size w x h (the

@@ -606,11 +606,17 @@ __device__ __forceinline__ void v_inverse2(f2 A, f2 B, f2 &o, f2 &e1, f2 &o1, f2
 // HH rows of H-row rb/2 (ra, rb the mirrored interleaved rows 2m, 2m+1); the
 // horizontal inverse rebuilds both interleaved rows, the vertical recurrence
 // emits output rows 2(m-LAT), 2(m-LAT)+1.  The band rows are staged from
-// band column B/2 on, `band_win` columns wide, `slot_i` floats per band-row
-// slot.
+// band column B/2 on, `band_win` columns wide.  Stage layout: band k (LL,
+// HL, LH, HH) at slot + k*kBandSlotF, its row for pair r at + r*kBandRowF,
+// band column c at offset c - (window start rounded down to 16 bytes).
+// With tensor maps (mll: LL band, mfr: the frame holding HL, LH, HH), an
+// interior unit stages each band's two consecutive rows of a stage with one
+// 68 x 2 box copy; stages with mirrored rows and edge units use one bulk
+// copy per band row.
 template <int NS, bool EDGE, class Pipe>
 __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
-                             int band_win, int slot_i, uint32_t &tick, int lane, int *err)
+                             int band_win, const CUtensorMap *mll, const CUtensorMap *mfr, uint32_t &tick,
+                             int lane, int *err)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
@@ -618,6 +624,7 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     const int bq = b >> 1;  // band column of lane 0's first value
     const int bqB = B >> 1;  // band column of the staged window's start
     const int Lw = (w + 1) >> 1, Hw = w >> 1;
+    const int hs = (h + 1) >> 1;
     int k0, total, iters;
     unit_span<NS>(D, seg, k0, total, iters);
     const int m0 = k0 - LAT;
@@ -631,10 +638,14 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     iHL.init(D.in[1], D.in_pitch[1], loH, hiH - loH);
     iLH.init(D.in[2], D.in_pitch[2], loL, hiL - loL);
     iHH.init(D.in[3], D.in_pitch[3], loH, hiH - loH);
-    const uint32_t tx = 2 * (iLL.bytes + iHL.bytes + iLH.bytes + iHH.bytes);
+    const uint32_t tx1 = 2 * (iLL.bytes + iHL.bytes + iLH.bytes + iHH.bytes);
+    // box copies: interior units only (their windows start at or after
+    // column 0 and the box's 16-byte aligned x is that window start)
+    const bool boxes = !EDGE && mll != nullptr && mfr != nullptr;
+    constexpr uint32_t kBoxBytes = kBandRowF * 2 * 4;
 
-    // this lane's offsets inside a pair's 4 band-row slots: even samples from
-    // the L bands (slots 0, 2), odd samples from the H bands (slots 1, 3)
+    // this lane's offsets inside a stage: even samples from the L bands
+    // (LL / LH slots), odd samples from the H bands (HL / HH slots)
     int offA[4], offB[4];
     if (EDGE) {
 #pragma unroll
@@ -648,15 +659,15 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
             const int lo_k = k ? loH : loL;
             const int oa = bi - lo_k + (k ? iHL.shift : iLL.shift);
             const int ob = bi - lo_k + (k ? iHH.shift : iLH.shift);
-            offA[i] = k * slot_i + min(max(oa, 0), slot_i - 1);
-            offB[i] = (2 + k) * slot_i + min(max(ob, 0), slot_i - 1);
+            offA[i] = k * kBandSlotF + min(max(oa, 0), kBandRowF - 1);
+            offB[i] = (2 + k) * kBandSlotF + min(max(ob, 0), kBandRowF - 1);
         }
     } else {
         const int d = bq - loL + 2 * lane;
         offA[0] = d + iLL.shift;
-        offA[1] = slot_i + d + iHL.shift;
-        offB[0] = 2 * slot_i + d + iLH.shift;
-        offB[1] = 3 * slot_i + d + iHH.shift;
+        offA[1] = kBandSlotF + d + iHL.shift;
+        offB[0] = 2 * kBandSlotF + d + iLH.shift;
+        offB[1] = 3 * kBandSlotF + d + iHH.shift;
     }
 
     const uint32_t t0 = tick;
@@ -666,19 +677,29 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
         if (!pipe.acquire(t)) return false;
         float *slot = pipe.slot(t);
         uint64_t *bar = pipe.bar(t);
+        const int m = m0 + 2 * u;  // first pair of the stage
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(bar, tx);
+        if (boxes && m >= 0 && 2 * m + 3 < h) {
+            // both pairs interior: band rows m and m + 1 of every band
+            mbar_arrive_expect_tx(bar, 4 * kBoxBytes);
+            tma_load_2d(slot, mll, loL - iLL.shift, m, bar);
+            tma_load_2d(slot + kBandSlotF, mfr, Lw + loH - iHL.shift, m, bar);
+            tma_load_2d(slot + 2 * kBandSlotF, mfr, loL - iLH.shift, hs + m, bar);
+            tma_load_2d(slot + 3 * kBandSlotF, mfr, Lw + loH - iHH.shift, hs + m, bar);
+            return true;
+        }
+        mbar_arrive_expect_tx(bar, tx1);
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
             int ra, rb;
-            pair_rows(m0 + 2 * u + r, h, ra, rb);
+            pair_rows(m + r, h, ra, rb);
             const int qa = ra >> 1, qb = rb >> 1;
-            float *sl = slot + 4 * r * slot_i;
+            float *sl = slot + r * kBandRowF;
             bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, bar);
-            bulk_g2s(sl + 2 * slot_i, iLH.base + qb * iLH.pitch, iLH.bytes, bar);
+            bulk_g2s(sl + 2 * kBandSlotF, iLH.base + qb * iLH.pitch, iLH.bytes, bar);
             if (iHL.bytes) {
-                bulk_g2s(sl + slot_i, iHL.base + qa * iHL.pitch, iHL.bytes, bar);
-                bulk_g2s(sl + 3 * slot_i, iHH.base + qb * iHH.pitch, iHH.bytes, bar);
+                bulk_g2s(sl + kBandSlotF, iHL.base + qa * iHL.pitch, iHL.bytes, bar);
+                bulk_g2s(sl + 3 * kBandSlotF, iHH.base + qb * iHH.pitch, iHH.bytes, bar);
             }
         }
         return true;
@@ -715,7 +736,7 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
         f2 E[4], O[4];  // interleaved rows: pair 0 L-row, H-row, pair 1 L-row, H-row
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-            const float *sl = slot + 4 * r * slot_i;
+            const float *sl = slot + r * kBandRowF;
             if (EDGE) {
                 E[2 * r] = pk(sl[offA[0]], sl[offA[2]]);
                 O[2 * r] = pk(sl[offA[1]], sl[offA[3]]);
@@ -796,7 +817,8 @@ __device__ __forceinline__ bool fast_ok(const LevelDesc &D)
 // private ring.
 template <int NS, bool INV>
 __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
-                                         uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch)
+                                         uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch,
+                                         const CUtensorMap *mll = nullptr, const CUtensorMap *mfr = nullptr)
 {
     if (D.h == 1 || D.rows_only)
         return INV ? inverse_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err)
@@ -805,8 +827,8 @@ __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, i
     const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
     const WarpPipe pipe{ring, bars};
     if (INV)
-        return edge ? inverse_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn / 2, kSlotI, tick, lane, err)
-                    : inverse_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn / 2, kSlotI, tick, lane, err);
+        return edge ? inverse_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn / 2, mll, mfr, tick, lane, err)
+                    : inverse_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn / 2, mll, mfr, tick, lane, err);
     return edge ? forward_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err)
                 : forward_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err);
 }
