@@ -202,7 +202,8 @@ batch_kernel(const BatchImage *__restrict__ imgs, const BatchItem *__restrict__ 
                            : level_item<2, false>(I, it.level, it.unit, ring, bars, tick, lane, err);
         }
         if (!ok) break;
-        __threadfence();
+        // the warp's stores, then one release by lane 0 (cumulative over the
+        // warp's writes ordered before it by the warp barrier)
         __syncwarp();
         if (lane == 0) {
             __threadfence();
