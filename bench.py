@@ -473,7 +473,8 @@ def serve_trace(seconds: float, rate: float = 20000.0, seed: int = 11):
 
 def run_serve_extra(D, torch, seconds: float):
     """Serving loop: a 20k req/s Poisson stream replayed in real time against
-    the continuous-batching server (64 GiB admission budget, pooled buffers);
+    the continuous-batching server (64 GiB admission budget, pooled buffers,
+    8 streams);
     every request reads its w x h input from a resident synthetic image and
     writes its result to a pooled buffer."""
     from libdwt_gb300 import synth
@@ -485,7 +486,7 @@ def run_serve_extra(D, torch, seconds: float):
     torch.cuda.synchronize()
     reqs = [D.Server.request(src, None, "cdf97" if wav[k] == 0 else "cdf53", bool(inv[k]), int(j[k]), tag=k,
                              w=int(w[k]), h=int(h[k])) for k in range(len(t))]
-    srv = D.Server(budget_bytes=64 << 30, n_streams=4)
+    srv = D.Server(budget_bytes=64 << 30, n_streams=8)
     t0 = time.perf_counter()
     lat = srv.replay(t, reqs, timeout_s=600)
     wall = time.perf_counter() - t0

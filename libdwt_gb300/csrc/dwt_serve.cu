@@ -5,10 +5,13 @@
 //   - admits pending requests in arrival order while their device memory
 //     (pooled output buffer if the client gave none, plus the inter-level
 //     scratch) fits the memory budget and an in-flight slot is free;
-//   - turns everything admitted since the last launch into one micro-batch:
-//     descriptors and work items of the batched persistent kernel, launched on
-//     the next of several streams, so micro-batches overlap on the device
-//     and requests that arrive while others run join the next one;
+//   - turns everything admitted since the last launch into one micro-batch
+//     on the next of several streams, so micro-batches overlap on the device
+//     and requests that arrive while others run join the next one: the small
+//     requests become descriptors and work items of the batched persistent
+//     kernel, the large ones (kDenseMinPixels and up, most of the pixels of
+//     a mixed stream) run the per-level pipeline of the plain drop-in, which
+//     is at its best on large images;
 //   - polls the micro-batches' completion events, returns their buffers to
 //     the pool (they stay cached there, not freed) and stamps each request's
 //     completion time.
@@ -91,6 +94,15 @@ size_t request_bytes(const dwt_gpu_request &r, int J)
     return sf * 4 + 256 + (r.dst ? 0 : size_t(r.w) * r.h * 4 + 256);
 }
 
+// Requests of at least this many pixels take the per-level pipeline.
+constexpr long long kDenseMinPixels = 1LL << 21;
+// A micro-batch takes requests until it holds this many pixels (about 0.3 ms
+// of GPU work): long micro-batches would leave the other streams idle while
+// the last of their work drains, and hold every request to the slowest.
+constexpr long long kFlightPixels = 1LL << 27;
+
+bool dense_request(const dwt_gpu_request &r) { return (long long)r.w * r.h >= kDenseMinPixels; }
+
 int levels_of(const dwt_gpu_request &r)
 {
     const int lim = dwt::ceil_log2_int(r.decompose_one ? std::max(r.w, r.h) : std::min(r.w, r.h));
@@ -101,20 +113,26 @@ int levels_of(const dwt_gpu_request &r)
 void launch_flight(dwt_gpu_server *S, Flight &f)
 {
     dwt::Context &c = dwt::ctx();
-    std::vector<BatchImage> imgs(f.reqs.size());
+    std::vector<BatchImage> imgs;
+    imgs.reserve(f.reqs.size());
     std::vector<std::vector<BatchItem>> by_phase(dwt::kPhases);
-    std::vector<int> copies;
+    std::vector<int> copies, dense;
     for (size_t i = 0; i < f.reqs.size(); ++i) {
         Req &q = f.reqs[i];
+        if (dense_request(q.r) && levels_of(q.r) > 0) {
+            dense.push_back(int(i));
+            continue;
+        }
         dwt_gpu_batch_image u{q.r.src, q.r.src_pitch_bytes,
                               q.r.dst ? q.r.dst : q.pooled,
                               q.r.dst ? q.r.dst_pitch_bytes : (long long)q.r.w * 4,
                               q.r.w, q.r.h, q.r.j_levels, q.r.decompose_one, q.r.wavelet, q.r.inverse};
-        dwt::plan_image(imgs[i], u, S->params, int(i), by_phase);
-        if (imgs[i].J == 0)
+        imgs.emplace_back();
+        dwt::plan_image(imgs.back(), u, S->params, int(imgs.size() - 1), by_phase);
+        if (imgs.back().J == 0)
             copies.push_back(int(i));
         else
-            dwt::set_image_scratch(imgs[i], static_cast<float *>(q.scratch));
+            dwt::set_image_scratch(imgs.back(), static_cast<float *>(q.scratch));
     }
     size_t n_items = 0;
     for (auto &v : by_phase) n_items += v.size();
@@ -152,6 +170,18 @@ void launch_flight(dwt_gpu_server *S, Flight &f)
         const int grid = std::max(1, std::min(c.sm_count * S->params.ctas_per_sm, int((n_items + 3) / 4)));
         dwt::launch_batch_kernel(grid, reinterpret_cast<BatchImage *>(d), reinterpret_cast<BatchItem *>(d + off_items),
                                  int(n_items), reinterpret_cast<int *>(d + off_cnt), c.d_err, f.stream);
+    }
+    for (int i : dense) {
+        Req &q = f.reqs[i];
+        float *dst = q.r.dst ? q.r.dst : q.pooled;
+        const long long dp = (q.r.dst ? q.r.dst_pitch_bytes : (long long)q.r.w * 4) / 4;
+        const int J = levels_of(q.r);
+        const cudaError_t e =
+            q.r.inverse ? dwt::dense_inverse(q.r.src, q.r.src_pitch_bytes / 4, dst, dp, q.r.w, q.r.h, J, q.r.wavelet,
+                                             static_cast<float *>(q.scratch), f.stream, c.d_err, 0)
+                        : dwt::dense_forward(q.r.src, q.r.src_pitch_bytes / 4, dst, dp, q.r.w, q.r.h, J, q.r.wavelet,
+                                             static_cast<float *>(q.scratch), f.stream, c.d_err, 0);
+        if (e != cudaSuccess) q.status = DWT_GPU_ECUDA;
     }
     cudaEventRecord(f.done, f.stream);
     f.busy = true;
@@ -199,11 +229,13 @@ void dispatcher_loop(dwt_gpu_server *S)
         }
         if (free_f) {
             std::unique_lock<std::mutex> g(S->mu);
-            while (!S->pending.empty()) {
+            long long flight_px = 0;
+            while (!S->pending.empty() && flight_px < kFlightPixels) {
                 Req &q = S->pending.front();
                 const int J = levels_of(q.r);
                 const size_t need = request_bytes(q.r, J);
                 if (S->used + need > S->budget) break;
+                flight_px += (long long)q.r.w * q.r.h;
                 q.bytes = need;
                 S->used += need;
                 S->peak = std::max(S->peak, S->used.load());

@@ -20,11 +20,14 @@ def env():
 def test_same_alone_and_in_mix(env):
     D, torch = env
     rng = np.random.default_rng(21)
-    src_big = torch.from_numpy(rng.integers(0, 256, size=(1200, 1200)).astype(np.float32)).cuda()
+    src_big = torch.from_numpy(rng.integers(0, 256, size=(2600, 2600)).astype(np.float32)).cuda()
     srv = D.Server(budget_bytes=64 << 30, n_streams=4)
     tracked = []
     for k in range(300):
-        w, h = int(rng.integers(1, 1100)), int(rng.integers(1, 1100))
+        if k % 20 == 7:  # large requests take the per-level pipeline inside the server
+            w, h = int(rng.integers(1450, 2600)), int(rng.integers(1450, 2600))
+        else:
+            w, h = int(rng.integers(1, 1100)), int(rng.integers(1, 1100))
         wav = str(rng.choice(["cdf97", "cdf53"]))
         inv = bool(rng.integers(0, 2))
         j = int(rng.integers(1, 7))
