@@ -174,6 +174,14 @@ def cpu_checks(threads: int, main_img, main_coef, main_rec, checks: dict) -> dic
         ref4 = part.copy()
         O.batch_1d_cdf97(ref4, n, st, count, lanes, gs, 4, False, threads)
         out["c4_fwd_bit_exact_vs_float_restatement"] = bool(np.array_equal(gpu_part, ref4))
+        # the CPU baseline of C4: the float restatement over the same bank
+        # layout (OpenMP over signals), forward, on a slice of 1024 groups
+        bank = np.repeat(part, 16, axis=0)
+        t0 = time.perf_counter()
+        O.batch_1d_cdf97(bank, n, st, bank.shape[0] * lanes, lanes, gs, 4, False, threads)
+        dt = time.perf_counter() - t0
+        out["c4_cpu_fwd_gsamples_s"] = {"value": round(bank.size / dt / 1e9, 3), "cores": threads, "kind": "port",
+                                        "sample": f"{bank.shape[0] * lanes} signals of {n}"}
     return out
 
 
@@ -276,6 +284,10 @@ def main():
                     help="length of the serving replay in the extras")
     ap.add_argument("--image", type=int, default=16384,
                     help="image side (a smaller case for profiler captures)")
+    ap.add_argument("--only", choices=["c2", "c3", "c4"], default=None,
+                    help="run one secondary configuration alone and print its figures "
+                         "(for profiler captures)")
+    ap.add_argument("--c4-groups", type=int, default=8192, help="signal groups of C4 (8 signals each)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     global W, H, J, WORKLOAD, SERVE_SECONDS
@@ -295,6 +307,17 @@ def main():
 
     torch.cuda.set_device(local)
     D.lib()
+    if args.only:
+        stream = torch.cuda.current_stream()
+        checks = {}
+        if args.only == "c4":
+            res = run_signals_extra(D, torch, checks, groups=args.c4_groups)
+        elif args.only == "c2":
+            res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks)
+        else:
+            res = run_serve_extra(D, torch, SERVE_SECONDS)
+        print(json.dumps({"only": args.only, **res}), flush=True)
+        return
     img = synth_image()
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
