@@ -102,6 +102,45 @@ DWT_EXPORT void dwt_util_set_accel(int accel_type);
 DWT_EXPORT int dwt_util_ceil_log2(int x);
 DWT_EXPORT int dwt_util_pow2_ceil_log2(int x);
 
+/* ------------------------------------------------- coefficient layout helpers */
+
+/* src/libdwt.h:1124-1129: the four subbands of one decomposition level. */
+enum dwt_subbands { DWT_LL, DWT_HL, DWT_LH, DWT_HH };
+
+/* src/libdwt.h:1295-1300: how an image is placed in its frame. */
+enum dwt_array { DWT_ARR_SIMPLE, DWT_ARR_SPARSE, DWT_ARR_PACKED };
+
+/* src/libdwt.h:1134-1187 (src/libdwt.c:8153-8262): pointer to and size of
+ * subband `band` of level j_max in a transformed frame (the subband starts
+ * at the halved outer size, its extent is the halved inner size). */
+DWT_EXPORT void dwt_util_subband(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                                 int size_i_big_x, int size_i_big_y, int j_max, enum dwt_subbands band,
+                                 void **dst_ptr, int *dst_size_x, int *dst_size_y);
+DWT_EXPORT void dwt_util_subband_s(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                                   int size_i_big_x, int size_i_big_y, int j_max, enum dwt_subbands band,
+                                   void **dst_ptr, int *dst_size_x, int *dst_size_y);
+DWT_EXPORT void dwt_util_subband_d(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                                   int size_i_big_x, int size_i_big_y, int j_max, enum dwt_subbands band,
+                                   void **dst_ptr, int *dst_size_x, int *dst_size_y);
+
+/* src/libdwt.h:1307-1340 (src/libdwt.c:8620-8701): row stride (bytes, a
+ * power-of-two row, made prime when opt_stride), element stride and the
+ * outer / inner frame of an image of size_x x size_y in layout array_type. */
+DWT_EXPORT void dwt_util_get_sizes_s(enum dwt_array array_type, int size_x, int size_y, int opt_stride,
+                                     int *stride_x, int *stride_y, int *size_o_big_x, int *size_o_big_y,
+                                     int *size_i_big_x, int *size_i_big_y);
+DWT_EXPORT void dwt_util_get_sizes_d(enum dwt_array array_type, int size_x, int size_y, int opt_stride,
+                                     int *stride_x, int *stride_y, int *size_o_big_x, int *size_o_big_y,
+                                     int *size_i_big_x, int *size_i_big_y);
+
+/* src/libdwt.c:8072-8151: the "optimal" stride is the smallest number at
+ * least min_stride that passes the reference's base-2 Fermat test (so it
+ * may be a base-2 pseudoprime, as in the reference). */
+DWT_EXPORT int dwt_util_is_prime(int n);
+DWT_EXPORT int dwt_util_next_prime(int n);
+DWT_EXPORT int dwt_util_get_opt_stride(int min_stride);
+DWT_EXPORT int dwt_util_get_stride(int min_stride, int opt);
+
 /* ------------------------------------------------------------- extensions */
 
 /* Error codes of the dwt_gpu_* functions (0 = success). */

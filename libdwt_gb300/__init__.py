@@ -80,6 +80,10 @@ def lib():
             getattr(L, f"dwt_{w}_2i_s").argtypes = [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
             getattr(L, f"dwt_{w}_f_ex_stride_s").argtypes = [_vp, _vp, _vp, _vp, _i, _i]
             getattr(L, f"dwt_{w}_i_ex_stride_s").argtypes = [_vp, _vp, _vp, _vp, _i, _i]
+        L.dwt_util_subband_s.argtypes = [_vp] + [_i] * 8 + [C.POINTER(_vp), C.POINTER(_i), C.POINTER(_i)]
+        L.dwt_util_subband_s.restype = None
+        L.dwt_util_get_sizes_s.argtypes = [_i] * 4 + [C.POINTER(_i)] * 6
+        L.dwt_util_get_sizes_s.restype = None
         L.dwt_gpu_2f_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
         L.dwt_gpu_2i_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
         L.dwt_gpu_1_s.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
@@ -192,6 +196,32 @@ def dwt_util_set_accel(accel_type: int) -> None:
 
 
 # ------------------------------------------------------------ conveniences
+
+DWT_LL, DWT_HL, DWT_LH, DWT_HH = range(4)
+DWT_ARR_SIMPLE, DWT_ARR_SPARSE, DWT_ARR_PACKED = range(3)
+
+
+def dwt_util_subband_s(ptr, stride_x: int, stride_y: int, size_o_big_x: int, size_o_big_y: int,
+                       size_i_big_x: int, size_i_big_y: int, j_max: int, band: int):
+    """Address (int) and (width, height) of subband `band` (DWT_LL, DWT_HL,
+    DWT_LH, DWT_HH) of level j_max in a transformed frame at `ptr`
+    (src/libdwt.c:8153-8262)."""
+    L = lib()
+    p, w, h = C.c_void_p(), C.c_int(), C.c_int()
+    L.dwt_util_subband_s(C.c_void_p(_addr(ptr)), stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+                         size_i_big_y, j_max, band, C.byref(p), C.byref(w), C.byref(h))
+    return int(p.value or 0), w.value, h.value
+
+
+def dwt_util_get_sizes_s(array_type: int, size_x: int, size_y: int, opt_stride: int):
+    """(stride_x, stride_y, size_o_big_x, size_o_big_y, size_i_big_x,
+    size_i_big_y) of a float image in layout `array_type`
+    (src/libdwt.c:8620-8659)."""
+    L = lib()
+    v = [C.c_int() for _ in range(6)]
+    L.dwt_util_get_sizes_s(array_type, size_x, size_y, opt_stride, *[C.byref(t) for t in v])
+    return tuple(t.value for t in v)
+
 
 def transform2(buf, wavelet, direction: str, stride_x: int, stride_y: int, size_o, size_i,
                j_max: int, decompose_one: int = 0, zero_padding: int = 0) -> int:
