@@ -84,6 +84,47 @@ DWT_EXPORT void dwt_cdf53_f_s(const float *src, float *dst, float *tmp, int N);
 DWT_EXPORT void dwt_cdf97_i_s(const float *src, float *dst, float *tmp, int N);
 DWT_EXPORT void dwt_cdf53_i_s(const float *src, float *dst, float *tmp, int N);
 
+/* --------------------------------------------------------- double precision */
+
+/* src/libdwt.h:455-486, 527-558 (src/libdwt.c:6120-6284, 6493-6645): the
+ * 2D drivers in double, same frame and level semantics as the float ones.
+ * Run on the GPU's FP64 units through the general per-line path: for
+ * completeness and FP64 checks, not throughput. */
+DWT_EXPORT void dwt_cdf97_2f_d(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                               int size_i_big_x, int size_i_big_y, int *j_max_ptr, int decompose_one,
+                               int zero_padding);
+DWT_EXPORT void dwt_cdf53_2f_d(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                               int size_i_big_x, int size_i_big_y, int *j_max_ptr, int decompose_one,
+                               int zero_padding);
+DWT_EXPORT void dwt_cdf97_2i_d(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                               int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                               int zero_padding);
+DWT_EXPORT void dwt_cdf53_2i_d(void *ptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                               int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                               int zero_padding);
+
+/* src/libdwt.h:191-212, 299-320 (src/libdwt.c:1467-1571, 5673-5777): one
+ * 1D level in double, samples `stride` bytes apart; tmp is not used. */
+DWT_EXPORT void dwt_cdf97_f_ex_stride_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N,
+                                        int stride);
+DWT_EXPORT void dwt_cdf53_f_ex_stride_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N,
+                                        int stride);
+DWT_EXPORT void dwt_cdf97_i_ex_stride_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N,
+                                        int stride);
+DWT_EXPORT void dwt_cdf53_i_ex_stride_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N,
+                                        int stride);
+
+/* src/libdwt.h:139-158, 247-266, 29-106: the contiguous and the
+ * concatenated (deprecated) forms in double. */
+DWT_EXPORT void dwt_cdf97_f_ex_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N);
+DWT_EXPORT void dwt_cdf53_f_ex_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N);
+DWT_EXPORT void dwt_cdf97_i_ex_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N);
+DWT_EXPORT void dwt_cdf53_i_ex_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N);
+DWT_EXPORT void dwt_cdf97_f_d(const double *src, double *dst, double *tmp, int N);
+DWT_EXPORT void dwt_cdf53_f_d(const double *src, double *dst, double *tmp, int N);
+DWT_EXPORT void dwt_cdf97_i_d(const double *src, double *dst, double *tmp, int N);
+DWT_EXPORT void dwt_cdf53_i_d(const double *src, double *dst, double *tmp, int N);
+
 /* ----------------------------------------------------------------- lifecycle */
 
 /* src/libdwt.h:851 (src/libdwt.c:7466-7490): bring up the GPU context, the
@@ -174,6 +215,17 @@ DWT_EXPORT int dwt_gpu_2i_s(int wavelet, void *ptr, int stride_x, int stride_y, 
  * b = src_h, c_or_l = dst, h_or_null unused. */
 DWT_EXPORT int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float *c_or_l,
                 float *h_or_null, int N, int stride);
+
+/* The double-precision forms of the three calls above, returning an error
+ * code (dwt_cdf97_2f_d and friends abort instead, like libdwt). */
+DWT_EXPORT int dwt_gpu_2f_d(int wavelet, void *ptr, int stride_x, int stride_y, int size_o_big_x,
+                            int size_o_big_y, int size_i_big_x, int size_i_big_y, int *j_max_ptr,
+                            int decompose_one, int zero_padding);
+DWT_EXPORT int dwt_gpu_2i_d(int wavelet, void *ptr, int stride_x, int stride_y, int size_o_big_x,
+                            int size_o_big_y, int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                            int zero_padding);
+DWT_EXPORT int dwt_gpu_1_d(int wavelet, int inverse, const double *a, const double *b, double *c_or_l,
+                           double *h_or_null, int N, int stride);
 
 /* Device-resident, out-of-place, asynchronous dense 2D transform of a w x h
  * image (outer == inner): src and dst are device pointers with row pitches in

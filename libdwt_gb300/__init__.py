@@ -87,6 +87,9 @@ def lib():
         L.dwt_gpu_2f_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
         L.dwt_gpu_2i_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
         L.dwt_gpu_1_s.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
+        L.dwt_gpu_2f_d.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
+        L.dwt_gpu_2i_d.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
+        L.dwt_gpu_1_d.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
         L.dwt_gpu_2_dev.argtypes = [_i, _i, _vp, _ll, _vp, _ll, _i, _i, _i, _i, _vp]
         L.dwt_gpu_1_batch_s.argtypes = [_i, _i, _vp, _i, _i, _ll, _i, _ll, _i]
         L.dwt_gpu_level_dev.argtypes = [_i, _i, _i, _i, C.POINTER(_vp), C.POINTER(_ll),
@@ -262,6 +265,29 @@ def level_dev(wavelet, inverse: bool, w: int, h: int, ins, in_pitch_bytes, outs,
                                    arr(_vp, [_addr(x) for x in ins]), arr(_ll, in_pitch_bytes),
                                    arr(_vp, [_addr(x) for x in outs]), arr(_ll, out_pitch_bytes),
                                    stream))
+
+
+def transform2_d(buf, wavelet, direction: str, stride_x: int, stride_y: int, size_o, size_i,
+                 j_max: int, decompose_one: int = 0, zero_padding: int = 0) -> int:
+    """transform2 in double precision (libdwt's _2f_d / _2i_d)."""
+    w = _WAVELETS[wavelet]
+    ox, oy = size_o
+    ix, iy = size_i
+    if direction == "f":
+        j = C.c_int(j_max)
+        _check(lib().dwt_gpu_2f_d(w, _addr(buf), stride_x, stride_y, ox, oy, ix, iy, C.byref(j),
+                                  decompose_one, zero_padding))
+        return j.value
+    _check(lib().dwt_gpu_2i_d(w, _addr(buf), stride_x, stride_y, ox, oy, ix, iy, j_max,
+                              decompose_one, zero_padding))
+    return j_max
+
+
+def strided_1d_d(wavelet, inverse: bool, a, b, c, d, N: int, stride: int) -> None:
+    """strided_1d in double precision (libdwt's _ex_stride_d)."""
+    _check(lib().dwt_gpu_1_d(_WAVELETS[wavelet], 1 if inverse else 0, _addr(a),
+                             None if b is None else _addr(b), _addr(c),
+                             None if d is None else _addr(d), N, stride))
 
 
 def strided_1d(wavelet, inverse: bool, a, b, c, d, N: int, stride: int) -> None:

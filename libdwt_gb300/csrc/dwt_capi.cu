@@ -25,6 +25,7 @@
 #include "../../include/libdwt.h"
 #include "dwt_capi_internal.h"
 #include "dwt_coarse.cuh"
+#include "dwt_double.cuh"
 #include "dwt_generic.cuh"
 #include "dwt_signals.cuh"
 #include "dwt_level2d.cuh"
@@ -476,7 +477,7 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
 // Validates a caller frame; returns false (and logs) for layouts the
 // library does not take: non-positive sizes with levels to do, negative
 // strides, samples that overlap, an inner frame larger than the outer one.
-static bool frame_ok(int sx, int sy, int ox, int oy, int ix, int iy)
+static bool frame_ok(int sx, int sy, int ox, int oy, int ix, int iy, int elem = 4)
 {
     if (ox < 0 || oy < 0 || ix < 0 || iy < 0) {
         log_error("negative image size\n");
@@ -490,8 +491,8 @@ static bool frame_ok(int sx, int sy, int ox, int oy, int ix, int iy)
         log_error("strides must be positive (stride_x=%d, stride_y=%d)\n", sx, sy);
         return false;
     }
-    const bool rows = (long long)sy >= 4 && (long long)sx >= (long long)ox * sy;
-    const bool cols = (long long)sx >= 4 && (long long)sy >= (long long)oy * sx;
+    const bool rows = (long long)sy >= elem && (long long)sx >= (long long)ox * sy;
+    const bool cols = (long long)sx >= elem && (long long)sy >= (long long)oy * sx;
     if (!(rows || cols) && ox > 1 && oy > 1) {
         log_error("stride_x=%d / stride_y=%d make samples of a %dx%d frame overlap\n", sx, sy, ox, oy);
         return false;
@@ -630,6 +631,125 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
 }
 
 // ------------------------------------------------------------ 1D driver
+
+// The double-precision 2D call (libdwt's _2f_d / _2i_d): the frame's byte
+// span staged to the device, repacked to a compact double frame, the
+// reference's per-line level sequence in place (dense frames included), and
+// unpacked back.  Same level and frame semantics as run_2d.
+static int run_2d_d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, int oy, int ix, int iy, int *jp,
+                    int j_in, int decompose_one, int zero_padding)
+{
+    t_last_error = DWT_GPU_OK;
+    if (!frame_ok(sx, sy, ox, oy, ix, iy, 8)) return set_error(DWT_GPU_EINVAL);
+    const int omin = std::min(ox, oy), omax = std::max(ox, oy);
+    const int j_limit = (decompose_one ? omax : omin) > 0 ? ceil_log2_int(decompose_one ? omax : omin) : 0;
+    int J;
+    if (!inverse) {
+        if (*jp < 0 || *jp > j_limit) *jp = j_limit;
+        J = *jp;
+    } else {
+        J = j_limit;
+        if (j_in >= 0 && j_in < J) J = j_in;
+    }
+    if (J == 0 || ox == 0 || oy == 0) return DWT_GPU_OK;
+    if (!ptr) {
+        log_error("null image pointer\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const MemKind kind = classify(ptr);
+    const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
+    const long long P = align_up(ox, 16);  // compact pitch in doubles
+    const long long sb = (long long)(oy - 1) * sx + (long long)(ox - 1) * sy + 8;
+    Buf frame(size_t(P) * oy * 8 + 256, s), span;
+    if (!frame.p) return set_error(DWT_GPU_ENOMEM);
+    double *f = static_cast<double *>(frame.p);
+    const void *src = ptr;
+    if (!on_device) {
+        if (!span.alloc(size_t(sb) + 16, s)) return set_error(DWT_GPU_ENOMEM);
+        CK(cudaMemcpyAsync(span.p, ptr, size_t(sb), cudaMemcpyHostToDevice, s));
+        src = span.p;
+    }
+    CK(launch_repack_d(src, sx, sy, ox, oy, f, P, s));
+    const int lmax = std::max(ox, oy);
+    Buf tmp(size_t(lmax) * lmax * 8 + 256, s);
+    if (!tmp.p) return set_error(DWT_GPU_ENOMEM);
+    double *t = static_cast<double *>(tmp.p);
+    if (!inverse) {
+        for (int j = 0; j < J; ++j)
+            CK(level_forward_d(f, P, ceil_div_pow2(ox, j), ceil_div_pow2(oy, j), ceil_div_pow2(ox, j + 1),
+                               ceil_div_pow2(oy, j + 1), ceil_div_pow2(ix, j), ceil_div_pow2(iy, j), zero_padding,
+                               wavelet, t, s));
+    } else {
+        for (int j = J; j >= 1; --j)
+            CK(level_inverse_d(f, P, ceil_div_pow2(ox, j), ceil_div_pow2(oy, j), ceil_div_pow2(ox, j - 1),
+                               ceil_div_pow2(oy, j - 1), ceil_div_pow2(ix, j - 1), ceil_div_pow2(iy, j - 1),
+                               zero_padding, wavelet, t, s));
+    }
+    if (!on_device) {
+        CK(launch_unpack_d(f, P, span.p, sx, sy, ox, oy, s));
+        CK(cudaMemcpyAsync(ptr, span.p, size_t(sb), cudaMemcpyDeviceToHost, s));
+    } else {
+        CK(launch_unpack_d(f, P, ptr, sx, sy, ox, oy, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+// The double-precision strided 1D level (libdwt's _ex_stride_d): the samples
+// gathered into one compact line, transformed, scattered to dst_l / dst_h
+// (forward) or dst (inverse).
+static int run_1d_d(int wavelet, bool inverse, const double *a, const double *b, double *c_l, double *h_out,
+                    int N, int stride)
+{
+    t_last_error = DWT_GPU_OK;
+    if (N < 0 || stride == 0) {
+        log_error("invalid 1D arguments (N=%d, stride=%d)\n", N, stride);
+        return set_error(DWT_GPU_EINVAL);
+    }
+    if (N == 0) return DWT_GPU_OK;
+    if (stride < 8) {
+        log_error("stride %d smaller than a sample\n", stride);
+        return set_error(DWT_GPU_EINVAL);
+    }
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const int nl = (N + 1) / 2, nh = N / 2;
+    Buf line(size_t(N) * 8 + 256, s), tmp(size_t(N) * 8 + 256, s);
+    if (!line.p || !tmp.p) return set_error(DWT_GPU_ENOMEM);
+    double *x = static_cast<double *>(line.p);
+    // samples at `stride` bytes <-> a compact run (one row of `n` doubles)
+    auto gather = [&](const double *src, double *dst, int n) -> cudaError_t {
+        if (n == 0) return cudaSuccess;
+        const MemKind k = classify(src);
+        const bool dev = k == MemKind::Device || k == MemKind::Managed;
+        return cudaMemcpy2DAsync(dst, 8, src, stride, 8, n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 s);
+    };
+    auto scatter = [&](const double *src, double *dst, int n) -> cudaError_t {
+        if (n == 0) return cudaSuccess;
+        const MemKind k = classify(dst);
+        const bool dev = k == MemKind::Device || k == MemKind::Managed;
+        return cudaMemcpy2DAsync(dst, stride, src, 8, 8, n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 s);
+    };
+    if (!inverse) {
+        CK(gather(a, x, N));
+        CK(line_d(false, x, N, wavelet, static_cast<double *>(tmp.p), s));
+        CK(scatter(x, c_l, nl));
+        CK(scatter(x + nl, h_out, nh));
+    } else {
+        CK(gather(a, x, nl));
+        CK(gather(b, x + nl, nh));
+        CK(line_d(true, x, N, wavelet, static_cast<double *>(tmp.p), s));
+        CK(scatter(x, c_l, N));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
 
 int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l, float *h_out, int N,
            int stride)
@@ -877,6 +997,29 @@ int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float 
     return run_1d(wavelet, inverse != 0, a, b, c_or_l, h_or_null, N, stride);
 }
 
+int dwt_gpu_2f_d(int wavelet, void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy,
+                 int *j_max_ptr, int decompose_one, int zero_padding)
+{
+    if (!j_max_ptr || (wavelet != CDF97 && wavelet != CDF53)) return set_error(DWT_GPU_EINVAL);
+    return run_2d_d(wavelet, false, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, 0, decompose_one,
+                    zero_padding);
+}
+
+int dwt_gpu_2i_d(int wavelet, void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy,
+                 int j_max, int decompose_one, int zero_padding)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_2d_d(wavelet, true, ptr, stride_x, stride_y, ox, oy, ix, iy, nullptr, j_max, decompose_one,
+                    zero_padding);
+}
+
+int dwt_gpu_1_d(int wavelet, int inverse, const double *a, const double *b, double *c_or_l, double *h_or_null,
+                int N, int stride)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_1d_d(wavelet, inverse != 0, a, b, c_or_l, h_or_null, N, stride);
+}
+
 int dwt_gpu_2_dev(int wavelet, int inverse, const float *src, long long src_pitch_bytes, float *dst,
                   long long dst_pitch_bytes, int w, int h, int j_levels, int decompose_one, void *stream)
 {
@@ -1017,6 +1160,98 @@ void dwt_cdf97_i_s(const float *src, float *dst, float *tmp, int N)
 void dwt_cdf53_i_s(const float *src, float *dst, float *tmp, int N)
 {
     dwt_cdf53_i_ex_s(src, src + (N + 1) / 2, dst, tmp, N);
+}
+
+// ------------------------------------------------ double precision (_d)
+
+void dwt_cdf97_2f_d(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2f_d(CDF97, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, decompose_one, zero_padding));
+}
+
+void dwt_cdf53_2f_d(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2f_d(CDF53, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max_ptr, decompose_one, zero_padding));
+}
+
+void dwt_cdf97_2i_d(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int j_max,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2i_d(CDF97, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max, decompose_one, zero_padding));
+}
+
+void dwt_cdf53_2i_d(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int j_max,
+                    int decompose_one, int zero_padding)
+{
+    die_if(dwt_gpu_2i_d(CDF53, ptr, stride_x, stride_y, ox, oy, ix, iy, j_max, decompose_one, zero_padding));
+}
+
+void dwt_cdf97_f_ex_stride_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d_d(CDF97, false, src, nullptr, dst_l, dst_h, N, stride));
+}
+
+void dwt_cdf97_i_ex_stride_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N,
+                             int stride)
+{
+    (void)tmp;
+    die_if(run_1d_d(CDF97, true, src_l, src_h, dst, nullptr, N, stride));
+}
+
+void dwt_cdf53_f_ex_stride_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N, int stride)
+{
+    (void)tmp;
+    die_if(run_1d_d(CDF53, false, src, nullptr, dst_l, dst_h, N, stride));
+}
+
+void dwt_cdf53_i_ex_stride_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N,
+                             int stride)
+{
+    (void)tmp;
+    die_if(run_1d_d(CDF53, true, src_l, src_h, dst, nullptr, N, stride));
+}
+
+void dwt_cdf97_f_ex_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N)
+{
+    dwt_cdf97_f_ex_stride_d(src, dst_l, dst_h, tmp, N, sizeof(double));
+}
+
+void dwt_cdf53_f_ex_d(const double *src, double *dst_l, double *dst_h, double *tmp, int N)
+{
+    dwt_cdf53_f_ex_stride_d(src, dst_l, dst_h, tmp, N, sizeof(double));
+}
+
+void dwt_cdf97_i_ex_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N)
+{
+    dwt_cdf97_i_ex_stride_d(src_l, src_h, dst, tmp, N, sizeof(double));
+}
+
+void dwt_cdf53_i_ex_d(const double *src_l, const double *src_h, double *dst, double *tmp, int N)
+{
+    dwt_cdf53_i_ex_stride_d(src_l, src_h, dst, tmp, N, sizeof(double));
+}
+
+void dwt_cdf97_f_d(const double *src, double *dst, double *tmp, int N)
+{
+    dwt_cdf97_f_ex_d(src, dst, dst + (N + 1) / 2, tmp, N);
+}
+
+void dwt_cdf53_f_d(const double *src, double *dst, double *tmp, int N)
+{
+    dwt_cdf53_f_ex_d(src, dst, dst + (N + 1) / 2, tmp, N);
+}
+
+void dwt_cdf97_i_d(const double *src, double *dst, double *tmp, int N)
+{
+    dwt_cdf97_i_ex_d(src, src + (N + 1) / 2, dst, tmp, N);
+}
+
+void dwt_cdf53_i_d(const double *src, double *dst, double *tmp, int N)
+{
+    dwt_cdf53_i_ex_d(src, src + (N + 1) / 2, dst, tmp, N);
 }
 
 void dwt_util_init(void) { (void)ctx(); }
