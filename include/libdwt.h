@@ -17,6 +17,9 @@
 #ifndef LIBDWT_GB300_H
 #define LIBDWT_GB300_H
 
+#include <stdint.h>
+#include <stdio.h>
+
 #if defined(__GNUC__)
 #define DWT_EXPORT __attribute__((visibility("default")))
 #else
@@ -173,6 +176,85 @@ DWT_EXPORT void dwt_util_get_sizes_s(enum dwt_array array_type, int size_x, int 
 DWT_EXPORT void dwt_util_get_sizes_d(enum dwt_array array_type, int size_x, int size_y, int opt_stride,
                                      int *stride_x, int *stride_y, int *size_o_big_x, int *size_o_big_y,
                                      int *size_i_big_x, int *size_i_big_y);
+
+/* ------------------------------------------ performance harness and helpers */
+
+/* src/libdwt.h:720-737, 753: timer types and their tick counter. */
+enum dwt_timer_types {
+    DWT_TIME_CLOCK_GETTIME,
+    DWT_TIME_CLOCK_GETTIME_REALTIME,
+    DWT_TIME_CLOCK_GETTIME_MONOTONIC,
+    DWT_TIME_CLOCK_GETTIME_MONOTONIC_RAW,
+    DWT_TIME_CLOCK_GETTIME_PROCESS_CPUTIME_ID,
+    DWT_TIME_CLOCK_GETTIME_THREAD_CPUTIME_ID,
+    DWT_TIME_CLOCK,
+    DWT_TIME_TIMES,
+    DWT_TIME_GETRUSAGE,
+    DWT_TIME_GETRUSAGE_SELF,
+    DWT_TIME_GETRUSAGE_CHILDREN,
+    DWT_TIME_GETRUSAGE_THREAD,
+    DWT_TIME_GETTIMEOFDAY,
+    DWT_TIME_IOCTL_RTC,
+    DWT_TIME_AUTOSELECT
+};
+typedef int64_t dwt_clock_t;
+
+/* src/libdwt.c:6834-7120: the timer the harness uses by default, a tick
+ * count and the ticks per second. */
+DWT_EXPORT int dwt_util_clock_autoselect(void);
+DWT_EXPORT dwt_clock_t dwt_util_get_clock(int type);
+DWT_EXPORT dwt_clock_t dwt_util_get_frequency(int type);
+
+/* src/libdwt.c:1140-1212: test pattern (type 0) and image allocation
+ * (malloc(stride_x * size_o_big_y), abort when it fails). */
+DWT_EXPORT void dwt_util_test_image_fill_s(void *ptr, int stride_x, int stride_y, int size_i_big_x,
+                                           int size_i_big_y, int rand);
+DWT_EXPORT void dwt_util_test_image_fill_d(void *ptr, int stride_x, int stride_y, int size_i_big_x,
+                                           int size_i_big_y, int rand);
+DWT_EXPORT void dwt_util_alloc_image(void **pptr, int stride_x, int stride_y, int size_o_big_x, int size_o_big_y);
+DWT_EXPORT void dwt_util_free_image(void **pptr);
+
+/* src/libdwt.c:1223-1277: 0 when two frames agree within 1e-3 (float) /
+ * 1e-6 (double) and hold no NaN or infinity, else 1. */
+DWT_EXPORT int dwt_util_compare_s(void *ptr1, void *ptr2, int stride_x, int stride_y, int size_i_big_x,
+                                  int size_i_big_y);
+DWT_EXPORT int dwt_util_compare_d(void *ptr1, void *ptr2, int stride_x, int stride_y, int size_i_big_x,
+                                  int size_i_big_y);
+
+/* src/libdwt.h:798-915: host thread controls of the CPU library; the GPU
+ * path is driven by one host thread (1, setting is accepted). */
+DWT_EXPORT int dwt_util_get_max_threads(void);
+DWT_EXPORT int dwt_util_get_num_threads(void);
+DWT_EXPORT int dwt_util_get_num_workers(void);
+DWT_EXPORT void dwt_util_set_num_threads(int num_threads);
+
+/* src/libdwt.c:8386-8617: M forward and M inverse transforms of M test
+ * images (this library's GPU path), N loops, the minimum of the
+ * per-transform averages in seconds. */
+DWT_EXPORT void dwt_util_perf_cdf97_2_s(int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                                        int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                                        int zero_padding, int M, int N, int clock_type, float *fwd_secs,
+                                        float *inv_secs);
+DWT_EXPORT void dwt_util_perf_cdf97_2_d(int stride_x, int stride_y, int size_o_big_x, int size_o_big_y,
+                                        int size_i_big_x, int size_i_big_y, int j_max, int decompose_one,
+                                        int zero_padding, int M, int N, int clock_type, double *fwd_secs,
+                                        double *inv_secs);
+
+/* src/libdwt.c:8703-9036: the harness over sizes min_x, ceil(1.28 x), ...,
+ * max_x (square images, or single rows for _1_), one "pixels<TAB>seconds"
+ * line per size into each file (gnuplot data, the reference's format). */
+DWT_EXPORT void dwt_util_measure_perf_cdf97_2_s(enum dwt_array array_type, int min_x, int max_x, int opt_stride,
+                                                int j_max, int decompose_one, int zero_padding, int M, int N,
+                                                int clock_type, FILE *fwd_plot_data, FILE *inv_plot_data);
+DWT_EXPORT void dwt_util_measure_perf_cdf97_2_d(enum dwt_array array_type, int min_x, int max_x, int opt_stride,
+                                                int j_max, int decompose_one, int zero_padding, int M, int N,
+                                                int clock_type, FILE *fwd_plot_data, FILE *inv_plot_data);
+DWT_EXPORT void dwt_util_measure_perf_cdf97_1_s(enum dwt_array array_type, int min_x, int max_x, int opt_stride,
+                                                int j_max, int decompose_one, int zero_padding, int M, int N,
+                                                int clock_type, FILE *fwd_plot_data, FILE *inv_plot_data);
+DWT_EXPORT void dwt_util_measure_perf_cdf97_1_d(enum dwt_array array_type, int min_x, int max_x, int opt_stride,
+                                                int j_max, int decompose_one, int zero_padding, int M, int N,
+                                                int clock_type, FILE *fwd_plot_data, FILE *inv_plot_data);
 
 /* src/libdwt.c:8072-8151: the "optimal" stride is the smallest number at
  * least min_stride that passes the reference's base-2 Fermat test (so it
