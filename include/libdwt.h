@@ -298,6 +298,16 @@ DWT_EXPORT int dwt_gpu_2i_s(int wavelet, void *ptr, int stride_x, int stride_y, 
 DWT_EXPORT int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float *c_or_l,
                 float *h_or_null, int N, int stride);
 
+/* Every channel of a dense interleaved float image (pixel = `channels`
+ * floats, rows stride_x bytes apart: the layout the reference's OpenCV
+ * wrapper transforms channel by channel, src/cvdwt.cpp:67-147), in place, in
+ * one call with one copy of the image each way.  The same result as
+ * dwt_cdf{97,53}_2{f,i}_s on each channel (ptr + 4c, stride_y = 4 *
+ * channels, outer = inner = w x h).  *j_levels: levels (< 0: the limit);
+ * the forward writes back the levels it ran. */
+DWT_EXPORT int dwt_gpu_2_channels_s(int wavelet, int inverse, void *ptr, int stride_x, int channels, int w, int h,
+                                    int *j_levels, int decompose_one);
+
 /* The double-precision forms of the three calls above, returning an error
  * code (dwt_cdf97_2f_d and friends abort instead, like libdwt). */
 DWT_EXPORT int dwt_gpu_2f_d(int wavelet, void *ptr, int stride_x, int stride_y, int size_o_big_x,

@@ -87,6 +87,7 @@ def lib():
         L.dwt_gpu_2f_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
         L.dwt_gpu_2i_s.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
         L.dwt_gpu_1_s.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
+        L.dwt_gpu_2_channels_s.argtypes = [_i, _i, _vp, _i, _i, _i, _i, C.POINTER(_i), _i]
         L.dwt_gpu_2f_d.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, C.POINTER(_i), _i, _i]
         L.dwt_gpu_2i_d.argtypes = [_i, _vp, _i, _i, _i, _i, _i, _i, _i, _i, _i]
         L.dwt_gpu_1_d.argtypes = [_i, _i, _vp, _vp, _vp, _vp, _i, _i]
@@ -265,6 +266,16 @@ def level_dev(wavelet, inverse: bool, w: int, h: int, ins, in_pitch_bytes, outs,
                                    arr(_vp, [_addr(x) for x in ins]), arr(_ll, in_pitch_bytes),
                                    arr(_vp, [_addr(x) for x in outs]), arr(_ll, out_pitch_bytes),
                                    stream))
+
+
+def transform2_channels(buf, wavelet, inverse: bool, stride_x: int, channels: int, w: int, h: int,
+                        j_levels: int = -1, decompose_one: int = 0) -> int:
+    """Every channel of a dense interleaved float image in one call
+    (dwt_gpu_2_channels_s); returns the levels run."""
+    j = C.c_int(j_levels)
+    _check(lib().dwt_gpu_2_channels_s(_WAVELETS[wavelet], 1 if inverse else 0, _addr(buf), stride_x, channels, w, h,
+                                      C.byref(j), decompose_one))
+    return j.value
 
 
 def transform2_d(buf, wavelet, direction: str, stride_x: int, stride_y: int, size_o, size_i,

@@ -907,6 +907,71 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
     return set_error(check_device_error(c));
 }
 
+// Every channel of a dense interleaved float image in one call: one copy of
+// the image each way, the channels split into compact planes, the level
+// pipeline per plane, and interleaved back.  The same bits as the drop-in
+// on each channel (ptr + 4c, stride_y = 4 * channels).
+static int run_2d_channels(int wavelet, bool inverse, void *ptr, int stride_x, int channels, int w, int h,
+                           int *j_levels, int decompose_one)
+{
+    t_last_error = DWT_GPU_OK;
+    if (!ptr || !j_levels || channels < 1 || w < 0 || h < 0 || (long long)stride_x < 4LL * channels * w ||
+        (reinterpret_cast<uintptr_t>(ptr) & 3) != 0) {
+        log_error("invalid interleaved 2D arguments\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+    const int lim = (decompose_one ? std::max(w, h) : std::min(w, h)) > 0
+                        ? ceil_log2_int(decompose_one ? std::max(w, h) : std::min(w, h))
+                        : 0;
+    int J;
+    if (!inverse) {
+        if (*j_levels < 0 || *j_levels > lim) *j_levels = lim;
+        J = *j_levels;
+    } else {
+        J = (*j_levels < 0 || *j_levels > lim) ? lim : *j_levels;
+    }
+    if (J == 0 || w == 0 || h == 0) return DWT_GPU_OK;
+    Context &c = ctx();
+    std::lock_guard<std::mutex> g(c.call_mu);
+    cudaStream_t s = c.stream;
+    const MemKind kind = classify(ptr);
+    const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
+    const long long rowb = 4LL * channels * w;
+    const long long P = align_up(w, 32);
+    const long long plane = P * h + 64;
+    Buf stage, in(size_t(plane) * channels * 4 + 256, s), out(size_t(plane) * channels * 4 + 256, s);
+    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
+    const void *src = ptr;
+    long long src_pitch = stride_x;
+    if (!on_device) {
+        if (!stage.alloc(size_t(rowb) * h + 256, s)) return set_error(DWT_GPU_ENOMEM);
+        CK(cudaMemcpy2DAsync(stage.p, rowb, ptr, stride_x, rowb, h, cudaMemcpyHostToDevice, s));
+        src = stage.p;
+        src_pitch = rowb;
+    }
+    CK(launch_deinterleave(src, src_pitch, channels, w, h, in.f(), P, plane, s));
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(w, h, J, &p0, &p1);
+    Buf scratch(sf * 4 + 256, s);
+    if (sf && !scratch.p) return set_error(DWT_GPU_ENOMEM);
+    for (int ch = 0; ch < channels; ++ch) {
+        const float *pin = in.f() + ch * plane;
+        float *pout = out.f() + ch * plane;
+        if (!inverse)
+            CK(dense_forward(pin, P, pout, P, w, h, J, wavelet, scratch.f(), s, c.d_err, 0));
+        else
+            CK(dense_inverse(pin, P, pout, P, w, h, J, wavelet, scratch.f(), s, c.d_err, 0));
+    }
+    if (!on_device) {
+        CK(launch_interleave(out.f(), P, plane, channels, w, h, stage.p, rowb, s));
+        CK(cudaMemcpy2DAsync(ptr, stride_x, stage.p, rowb, rowb, h, cudaMemcpyDeviceToHost, s));
+    } else {
+        CK(launch_interleave(out.f(), P, plane, channels, w, h, ptr, stride_x, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
 int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_bytes, float *dst,
                long long dst_pitch_bytes, int w, int h, int j_levels, int decompose_one, cudaStream_t s)
 {
@@ -995,6 +1060,13 @@ int dwt_gpu_1_s(int wavelet, int inverse, const float *a, const float *b, float 
 {
     if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
     return run_1d(wavelet, inverse != 0, a, b, c_or_l, h_or_null, N, stride);
+}
+
+int dwt_gpu_2_channels_s(int wavelet, int inverse, void *ptr, int stride_x, int channels, int w, int h,
+                         int *j_levels, int decompose_one)
+{
+    if (wavelet != CDF97 && wavelet != CDF53) return set_error(DWT_GPU_EINVAL);
+    return run_2d_channels(wavelet, inverse != 0, ptr, stride_x, channels, w, h, j_levels, decompose_one);
 }
 
 int dwt_gpu_2f_d(int wavelet, void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy,

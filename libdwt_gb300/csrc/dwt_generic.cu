@@ -166,6 +166,32 @@ __global__ void zero_inverse_kernel(float *base, long long ls, long long es, int
     for (int i = N; i < n_dst; ++i) line[i * es] = 0.0f;
 }
 
+// Interleaved channels (pixel = `channels` floats) <-> one compact plane per
+// channel, plane c at planes + c * plane_stride (pitch in floats).
+__global__ void deinterleave_kernel(const unsigned char *src, long long src_pitch, int channels, int w, int h,
+                                    float *planes, long long pitch, long long plane_stride)
+{
+    const long long n = (long long)w * h * channels;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const long long row = k / ((long long)w * channels);
+        const int e = int(k - row * w * channels);  // float index within the row: x * channels + c
+        const int x = e / channels, c = e - x * channels;
+        planes[c * plane_stride + row * pitch + x] = load_any(src + row * src_pitch + (long long)e * 4);
+    }
+}
+
+__global__ void interleave_kernel(const float *planes, long long pitch, long long plane_stride, int channels, int w,
+                                  int h, unsigned char *dst, long long dst_pitch)
+{
+    const long long n = (long long)w * h * channels;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const long long row = k / ((long long)w * channels);
+        const int e = int(k - row * w * channels);
+        const int x = e / channels, c = e - x * channels;
+        store_any(dst + row * dst_pitch + (long long)e * 4, planes[c * plane_stride + row * pitch + x]);
+    }
+}
+
 int grid_for(long long n, int block)
 {
     long long g = (n + block - 1) / block;
@@ -191,6 +217,26 @@ cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long lo
     if ((long long)ox * oy == 0) return cudaSuccess;
     unpack_kernel<<<grid_for((long long)ox * oy, 256), 256, 0, s>>>(
         src, spitch, static_cast<unsigned char *>(dst), sx, sy, ox, oy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deinterleave(const void *src, long long src_pitch_bytes, int channels, int w, int h,
+                                float *planes, long long pitch, long long plane_stride, cudaStream_t s)
+{
+    const long long n = (long long)w * h * channels;
+    if (n == 0) return cudaSuccess;
+    deinterleave_kernel<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const unsigned char *>(src), src_pitch_bytes,
+                                                          channels, w, h, planes, pitch, plane_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interleave(const float *planes, long long pitch, long long plane_stride, int channels, int w,
+                              int h, void *dst, long long dst_pitch_bytes, cudaStream_t s)
+{
+    const long long n = (long long)w * h * channels;
+    if (n == 0) return cudaSuccess;
+    interleave_kernel<<<grid_for(n, 256), 256, 0, s>>>(planes, pitch, plane_stride, channels, w, h,
+                                                        static_cast<unsigned char *>(dst), dst_pitch_bytes);
     return cudaGetLastError();
 }
 

@@ -13,6 +13,14 @@ cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long lo
                           int ox, int oy, cudaStream_t s);
 
 // strided signal bank <-> compact rows (one signal per row)
+// Interleaved channels (pixel = `channels` floats, rows src_pitch_bytes
+// apart) <-> one compact plane per channel (plane c at planes + c *
+// plane_stride, row pitch `pitch` floats).
+cudaError_t launch_deinterleave(const void *src, long long src_pitch_bytes, int channels, int w, int h,
+                                float *planes, long long pitch, long long plane_stride, cudaStream_t s);
+cudaError_t launch_interleave(const float *planes, long long pitch, long long plane_stride, int channels, int w,
+                              int h, void *dst, long long dst_pitch_bytes, cudaStream_t s);
+
 cudaError_t launch_gather_signals(const void *base, int N, long long stride, long long count, int group,
                                   long long group_stride, long long lane_stride, float *dst,
                                   long long dpitch, cudaStream_t s);
