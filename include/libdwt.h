@@ -17,6 +17,7 @@
 #ifndef LIBDWT_GB300_H
 #define LIBDWT_GB300_H
 
+#include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -263,6 +264,96 @@ DWT_EXPORT int dwt_util_is_prime(int n);
 DWT_EXPORT int dwt_util_next_prime(int n);
 DWT_EXPORT int dwt_util_get_opt_stride(int min_stride);
 DWT_EXPORT int dwt_util_get_stride(int min_stride, int opt);
+
+/* ---------------------------------------------------- zero padding, stand-alone */
+
+/* src/libdwt.h:355-406 (src/libdwt.c:5872-5942): zeros in L at samples
+ * [ceil(N/2), N_dst_L) and in H at [floor(N/2), N_dst_H), `stride` bytes
+ * apart (sizeof the element for the unstrided forms).  Host, device or
+ * managed memory.  A destination shorter than its half writes nothing. */
+DWT_EXPORT void dwt_zero_padding_f_s(float *dst_l, float *dst_h, int N, int N_dst_L, int N_dst_H);
+DWT_EXPORT void dwt_zero_padding_f_d(double *dst_l, double *dst_h, int N, int N_dst_L, int N_dst_H);
+DWT_EXPORT void dwt_zero_padding_f_stride_s(float *dst_l, float *dst_h, int N, int N_dst_L, int N_dst_H,
+                                            int stride);
+DWT_EXPORT void dwt_zero_padding_f_stride_d(double *dst_l, double *dst_h, int N, int N_dst_L, int N_dst_H,
+                                            int stride);
+
+/* src/libdwt.h:409-453 (src/libdwt.c:5944-6004): zeros at samples [N, N_dst). */
+DWT_EXPORT void dwt_zero_padding_i_s(float *dst_l, int N, int N_dst);
+DWT_EXPORT void dwt_zero_padding_i_d(double *dst_l, int N, int N_dst);
+DWT_EXPORT void dwt_zero_padding_i_stride_s(float *dst_l, int N, int N_dst, int stride);
+DWT_EXPORT void dwt_zero_padding_i_stride_d(double *dst_l, int N, int N_dst, int stride);
+
+/* ------------------------------------------------ images, vectors, platform */
+
+/* src/libdwt.h:1190-1222 (src/libdwt.c:958-986): ptr + y*stride_x + x*stride_y. */
+DWT_EXPORT void *dwt_util_addr_coeff(void *ptr, int y, int x, int stride_x, int stride_y);
+DWT_EXPORT float *dwt_util_addr_coeff_s(void *ptr, int y, int x, int stride_x, int stride_y);
+DWT_EXPORT double *dwt_util_addr_coeff_d(void *ptr, int y, int x, int stride_x, int stride_y);
+
+/* src/libdwt.h:645 (src/libdwt.c:1180-1192): zero the inner frame (host memory). */
+DWT_EXPORT void dwt_util_test_image_zero_s(void *ptr, int stride_x, int stride_y, int size_i_big_x,
+                                           int size_i_big_y);
+
+/* src/libdwt.h:866-892 (src/libdwt.c:7532-7668): plain PGM ("P2", maxval
+ * 255) of the inner frame, pixel = 255 * px / max_value truncated, clamped
+ * to [0, 255]; 0 on success, 1 when the file cannot be written. */
+DWT_EXPORT int dwt_util_save_to_pgm_s(const char *filename, float max_value, const void *ptr, int stride_x,
+                                      int stride_y, int size_i_big_x, int size_i_big_y);
+DWT_EXPORT int dwt_util_save_to_pgm_d(const char *filename, double max_value, const void *ptr, int stride_x,
+                                      int stride_y, int size_i_big_x, int size_i_big_y);
+
+/* src/libdwt.h:1227-1250 (src/libdwt.c:8326-8384): dst = log(1 + 100|src|) / 10. */
+DWT_EXPORT void dwt_util_conv_show_s(const void *src, void *dst, int stride_x, int stride_y, int size_i_big_x,
+                                     int size_i_big_y);
+DWT_EXPORT void dwt_util_conv_show_d(const void *src, void *dst, int stride_x, int stride_y, int size_i_big_x,
+                                     int size_i_big_y);
+
+/* src/libdwt.h:961-1005 (src/libdwt.c:7716-7833): 8-byte aligned vector of an
+ * even number of floats; fill with 0, 1, ...; zero; copy; compare.  The int
+ * results are 0 when every element checks (normal or zero, within 1e-4). */
+DWT_EXPORT float *dwt_util_allocate_vec_s(int size);
+DWT_EXPORT int dwt_util_generate_vec_s(float *addr, int size);
+DWT_EXPORT int dwt_util_zero_vec_s(float *addr, int size);
+DWT_EXPORT int dwt_util_copy_vec_s(const float *src, float *dst, int size);
+DWT_EXPORT int dwt_util_cmp_vec_s(const float *a, const float *b, int size);
+
+/* src/libdwt.h:1010-1060 (src/libdwt.c:7921-7985): printf wrappers, and a
+ * log line to stderr behind the level's prefix ("DEBUG: ", "INFO: ",
+ * "WARNING: ", "ERROR: ", "TEST: "). */
+enum dwt_util_loglevel { LOG_NONE = 0, LOG_DBG, LOG_INFO, LOG_WARN, LOG_ERR, LOG_TEST };
+DWT_EXPORT int dwt_util_vfprintf(FILE *stream, const char *format, va_list ap);
+DWT_EXPORT int dwt_util_vprintf(const char *format, va_list ap);
+DWT_EXPORT int dwt_util_fprintf(FILE *stream, const char *format, ...);
+DWT_EXPORT int dwt_util_printf(const char *format, ...);
+DWT_EXPORT int dwt_util_log(enum dwt_util_loglevel level, const char *format, ...);
+
+/* src/libdwt.h:708-713, 1067-1083 (src/libdwt.c:507-520, 4918, 8014-8058):
+ * library version, architecture, 8-byte alignment test, host name and
+ * program name. */
+DWT_EXPORT const char *dwt_util_version(void);
+DWT_EXPORT const char *dwt_util_arch(void);
+DWT_EXPORT int dwt_util_is_aligned_8(const void *ptr);
+DWT_EXPORT const char *dwt_util_node(void);
+DWT_EXPORT const char *dwt_util_appname(void);
+
+/* src/libdwt.h:744-747 (src/libdwt.c:7259-7373): 0 when the timer type is
+ * available, else -1.  src/libdwt.h:950-955 (7375-7387): busy wait. */
+DWT_EXPORT int dwt_util_clock_available(int type);
+DWT_EXPORT void dwt_util_wait(int ms);
+
+/* src/libdwt.h:803-823, 899, 918-945 (src/libdwt.c:6006-6060, 7389-7436,
+ * 7512-7530, 7835-7919): worker and firmware controls of the reference's
+ * embedded accelerator (one worker here, the firmware switch is accepted),
+ * the OpenMP thread number (0: calls are not in a parallel region), abort,
+ * and the platform self-test (host vectors, then a device round trip). */
+enum dwt_op { DWT_OP_NONE, DWT_OP_LIFT4SA, DWT_OP_LIFT4SB };
+DWT_EXPORT int dwt_util_get_max_workers(void);
+DWT_EXPORT void dwt_util_set_num_workers(int num_workers);
+DWT_EXPORT int dwt_util_get_thread_num(void);
+DWT_EXPORT void dwt_util_switch_op(enum dwt_op op);
+DWT_EXPORT void dwt_util_abort(void);
+DWT_EXPORT void dwt_util_test(void);
 
 /* ------------------------------------------------------------- extensions */
 

@@ -24,7 +24,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # the product c*(l + r) before adding it, as the reference's float path does;
 # explicit .rn rounding alone did not keep packed f32x2 multiplies and adds
 # apart.
+# -ffp-contract=off: host code (the harness, the display transform) rounds
+# every product too, on both host architectures.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC",
+                     "-Xcompiler", "-ffp-contract=off",
                      "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 
 
