@@ -246,3 +246,33 @@ def test_zero_padding_on_device_memory(lib):
         else:
             getattr(L, f"dwt_zero_padding_i_stride_{g['t']}")(base, g["N"], g["nd"], g["stride"])
         assert buf.cpu().tolist() == g["out"]
+
+
+def _build_c_caller(lib_path, tmp_path):
+    src = os.path.join(ROOT, "tests", "c", "drop_in_roundtrip.c")
+    exe = str(tmp_path / "drop_in_roundtrip")
+    libdir = os.path.dirname(lib_path)
+    subprocess.run(["gcc", "-std=c99", "-O1", "-I", os.path.join(ROOT, "include"), src, "-o", exe, "-L", libdir,
+                    "-ldwt_gb300", f"-Wl,-rpath,{libdir}", "-Wl,--no-undefined", "-lm"], check=True,
+                   capture_output=True)
+    return exe
+
+
+def test_c_caller_builds_against_the_header(lib, tmp_path):
+    _, path = lib
+    assert os.path.exists(_build_c_caller(path, tmp_path))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("size", [(512, 512), (1023, 769)])
+def test_c_caller_round_trip_on_the_device(lib, tmp_path, size):
+    _, path = lib
+    exe = _build_c_caller(path, tmp_path)
+    pgm = str(tmp_path / "view.pgm")
+    r = subprocess.run([exe, str(size[0]), str(size[1]), pgm], capture_output=True, timeout=300)
+    err = r.stderr.decode()
+    assert r.returncode == 0, err
+    assert f"cdf97 {size[0]}x{size[1]}" in err and err.count("round trip: ok") == 2
+    with open(pgm) as f:
+        head = [f.readline().strip() for _ in range(3)]
+    assert head == ["P2", f"{size[0]} {size[1]}", "255"]
