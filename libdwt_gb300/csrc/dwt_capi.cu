@@ -69,8 +69,6 @@ Context &ctx()
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
         cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking);
         cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking);
-        for (auto &row : c->ev)
-            for (auto &e : row) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         cudaMalloc(&c->d_err, sizeof(int));
         cudaMemset(c->d_err, 0, sizeof(int));
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
@@ -87,8 +85,7 @@ void ctx_finish()
     cudaStreamSynchronize(g_ctx->stream);
     g_ctx->pool.release_all();
     cudaFree(g_ctx->d_err);
-    for (auto &row : g_ctx->ev)
-        for (auto &e : row) cudaEventDestroy(e);
+    for (cudaEvent_t e : g_ctx->events) cudaEventDestroy(e);
     cudaStreamDestroy(g_ctx->s_in);
     cudaStreamDestroy(g_ctx->s_out);
     cudaStreamDestroy(g_ctx->stream);
@@ -311,23 +308,153 @@ cudaError_t dense_inverse(const float *in, long long in_pitch, float *out, long 
 
 // A dense frame in host memory is copied in, transformed and copied out in
 // row bands on three streams, so that the copies in and out (full duplex over
-// the host link) overlap each other and the kernels.  Forward: band b of the
-// input rows is copied in, the level-0 segments whose rows (with the lifting
-// warm-up) are then present run, and their finished detail rows (HL of those
-// rows, LH and HH of the matching lower rows) are copied out at once; the
-// coarser levels follow on the small LL band and the top-left quadrant is
-// copied out last.  Inverse: the top-left quadrant (LL1 and every coarser
-// band) comes first, levels J..2 run, then level 1 runs band by band as its
-// detail rows arrive and its output rows leave.
-constexpr int kBands = 16;
+// the host link) overlap each other and the kernels.  The caller's frame is
+// both input and output: a copy out to host rows waits until the copy in has
+// read them.
+//
+// Forward: level-0 row bands run in order.  Each band reads its input rows
+// (with the lifting warm-up) and, ahead of need, the host rows its LH and HH
+// rows will overwrite, so the band's whole detail output can leave at once.
+// Level 1 runs band by band behind level 0 as its LL1 rows appear, and its
+// detail rows leave as soon as their host rows have been read; the levels
+// below run on the small LL2 band and its quadrant is copied out last.
+// Inverse: the top-left quadrant (LL1 and every coarser band) comes first,
+// levels J..2 run, then level 1 runs band by band as its detail rows arrive
+// and its output rows leave.
+constexpr int kInvBands = 16;
 constexpr long long kPipelineMinPixels = 1LL << 22;
 
-// A copy out to host rows [r0, r1) (columns [c0, c1)) waits until the copy
-// in has read those host rows: the caller's frame is both input and output.
-struct HostOut {
-    int r0, r1, c0, c1;  // host rows / columns
-    const float *src;    // device address of (r0, c0)
-    int ev;              // compute event it follows
+static int host_bands()
+{
+    static const int n = [] {
+        const char *e = getenv("DWT_GPU_HOST_BANDS");
+        const int v = e ? atoi(e) : 0;
+        return v >= 2 && v <= 256 ? v : 16;
+    }();
+    return n;
+}
+
+// Host rows of the caller's frame: which copy in read each row (columns
+// [0, split) and [split, W) separately), and the copies out waiting for
+// their rows.  Copy and band events come from the context's pool in order.
+struct HostRows {
+    Context &c;
+    cudaStream_t si, so;
+    char *host;
+    long long sx;
+    float *dev;
+    long long P;
+    int W, H, split;
+    int n_ev = 0;
+    std::vector<int> ev_of[2];  // pool index of the copy that read row r (per column part), -1: unread
+    struct Out {
+        int r0, r1, c0, c1;  // host rows / columns
+        const float *src;    // device address of (r0, c0), pitch P
+        int ev;              // band event it follows
+    };
+    std::vector<Out> pending;
+
+    HostRows(Context &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_)
+        : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), split(split_)
+    {
+        ev_of[0].assign(H, -1);
+        ev_of[1].assign(H, -1);
+    }
+
+    cudaError_t record(cudaStream_t st, int &idx)
+    {
+        idx = n_ev++;
+        cudaEvent_t e = c.event(idx);
+        return e ? cudaEventRecord(e, st) : cudaErrorMemoryAllocation;
+    }
+
+    // Copies in every unread part of rows [r0, r1) selected by `parts`
+    // (bit 0: columns [0, split), bit 1: [split, W)); one copy per run of
+    // rows that miss the same parts.
+    cudaError_t read(int r0, int r1, int parts = 3)
+    {
+        r0 = std::max(r0, 0);
+        r1 = std::min(r1, H);
+        if (split >= W) parts &= 1;
+        if (split <= 0) parts &= 2;
+        auto miss = [&](int r) {
+            return ((parts & 1) && ev_of[0][r] < 0 ? 1 : 0) | ((parts & 2) && ev_of[1][r] < 0 ? 2 : 0);
+        };
+        for (int r = r0; r < r1;) {
+            const int m = miss(r);
+            int e = r + 1;
+            while (e < r1 && miss(e) == m) ++e;
+            if (m) {
+                const int cb = (m & 1) ? 0 : split, ce = (m & 2) ? W : split;
+                cudaError_t err = cudaMemcpy2DAsync(dev + r * P + cb, P * 4, host + r * sx + cb * 4LL, sx,
+                                                    size_t(ce - cb) * 4, e - r, cudaMemcpyHostToDevice, si);
+                int idx = 0;
+                if (err == cudaSuccess) err = record(si, idx);
+                if (err != cudaSuccess) return err;
+                for (int k = r; k < e; ++k) {
+                    if (m & 1) ev_of[0][k] = idx;
+                    if (m & 2) ev_of[1][k] = idx;
+                }
+            }
+            r = e;
+        }
+        return cudaSuccess;
+    }
+
+    // Latest copy that read a selected part of rows [r0, r1); -2 if one of
+    // them is unread, -1 if none needed a copy.
+    int last_copy(int r0, int r1, int parts = 3) const
+    {
+        r0 = std::max(r0, 0);
+        r1 = std::min(r1, H);
+        if (split >= W) parts &= 1;
+        if (split <= 0) parts &= 2;
+        int last = -1;
+        for (int r = r0; r < r1; ++r)
+            for (int q = 0; q < 2; ++q)
+                if (parts & (1 << q)) {
+                    if (ev_of[q][r] < 0) return -2;
+                    last = std::max(last, ev_of[q][r]);
+                }
+        return last;
+    }
+
+    // Stream `st` waits until the selected parts of rows [r0, r1) are in.
+    cudaError_t wait_rows(cudaStream_t st, int r0, int r1, int parts = 3)
+    {
+        const int last = last_copy(r0, r1, parts);
+        if (last == -2) return cudaErrorInvalidValue;  // a scheduling bug: rows not read
+        return last >= 0 ? cudaStreamWaitEvent(st, c.event(last), 0) : cudaSuccess;
+    }
+
+    void out(int r0, int r1, int c0, int c1, const float *src, int ev)
+    {
+        if (r1 > r0 && c1 > c0) pending.push_back({r0, r1, c0, c1, src, ev});
+    }
+
+    // Issues every pending copy out whose host rows have been read (all of
+    // them when `all`: the caller has read every row by then).
+    cudaError_t flush(bool all)
+    {
+        size_t keep = 0;
+        for (size_t k = 0; k < pending.size(); ++k) {
+            const Out &o = pending[k];
+            const int last = last_copy(o.r0, o.r1);
+            if (last == -2) {
+                if (all) return cudaErrorInvalidValue;
+                pending[keep++] = o;
+                continue;
+            }
+            cudaError_t e = cudaStreamWaitEvent(so, c.event(o.ev), 0);
+            if (e == cudaSuccess && last >= 0) e = cudaStreamWaitEvent(so, c.event(last), 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpy2DAsync(host + o.r0 * sx + o.c0 * 4LL, sx, o.src, P * 4, size_t(o.c1 - o.c0) * 4,
+                                      o.r1 - o.r0, cudaMemcpyDeviceToHost, so);
+            if (e != cudaSuccess) return e;
+        }
+        pending.resize(keep);
+        return cudaSuccess;
+    }
 };
 
 static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
@@ -342,67 +469,90 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     float *buf[2];
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
+    HostRows R(c, host, sx, in.f(), P, W, H, W);
     // the pool may hand out blocks last used on `s`: let the copy streams wait
-    CK(cudaEventRecord(c.ev[0][63], s));
-    CK(cudaStreamWaitEvent(si, c.ev[0][63], 0));
-    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
+    int ev0 = 0;
+    CK(R.record(s, ev0));
+    CK(cudaStreamWaitEvent(si, c.event(ev0), 0));
+    CK(cudaStreamWaitEvent(so, c.event(ev0), 0));
 
     const int LAT = wavelet == CDF97 ? 2 : 1;
-    const int wd = (W + 1) / 2, hd = (H + 1) / 2, hh = H / 2;
-    LevelDesc d0 = fwd_desc(in.f(), P, out.f(), P, W, H, J, 0, buf, p);
+    float *const o = out.f();
+    // detail (and, at the last level, LL) output of level j's pairs [k0, k1)
+    auto emit = [&](int j, int k0, int k1, int ev) {
+        const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
+        const int wd = (w + 1) / 2, hd = (h + 1) / 2, hh = h / 2;
+        if (j == J - 1)
+            R.out(k0, k1, 0, w, o + k0 * P, ev);  // LL and HL
+        else
+            R.out(k0, k1, wd, w, o + k0 * P + wd, ev);  // HL
+        R.out(hd + k0, hd + std::min(k1, hh), 0, w, o + (hd + k0) * P, ev);  // LH, HH
+    };
+
+    LevelDesc d0 = fwd_desc(in.f(), P, o, P, W, H, J, 0, buf, p);
     plan_level(d0, 0, false);
-    const int npairs = (H + 1) / 2, seg = d0.seg_pairs, nsegs = d0.n_segs;
-    const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
-    std::vector<HostOut> pending;
-    int rows_in = 0, b = 0, last_in_ev = -1;
-    auto flush = [&](bool all) -> cudaError_t {
-        size_t k = 0;
-        for (; k < pending.size(); ++k) {
-            const HostOut &o = pending[k];
-            if (!all && o.r1 > rows_in) break;
-            cudaError_t e = cudaStreamWaitEvent(so, c.ev[1][o.ev], 0);
-            if (e == cudaSuccess && last_in_ev >= 0) e = cudaStreamWaitEvent(so, c.ev[0][last_in_ev], 0);
-            if (e == cudaSuccess)
-                e = cudaMemcpy2DAsync(host + o.r0 * sx + o.c0 * 4LL, sx, o.src, P * 4, size_t(o.c1 - o.c0) * 4,
-                                      o.r1 - o.r0, cudaMemcpyDeviceToHost, so);
+    const int np0 = (H + 1) / 2, hd0 = np0, hh0 = H / 2, nb = host_bands();
+    const int per0 = std::max(1, (d0.n_segs + nb - 1) / nb);
+    const bool lvl1 = J >= 2;
+    LevelDesc d1{};
+    int np1 = 0, per1 = 1, next1 = 0;
+    if (lvl1) {
+        d1 = fwd_desc(in.f(), P, o, P, W, H, J, 1, buf, p);
+        plan_level(d1, 0, false);
+        np1 = (d1.h + 1) / 2;
+        per1 = std::max(1, (d1.n_segs + nb / 2 - 1) / (nb / 2));
+    }
+    // level-1 segments whose LL1 rows (with the warm-up) are computed
+    auto run_level1 = [&](int done0) -> cudaError_t {
+        while (lvl1 && next1 < d1.n_segs) {
+            const int se = std::min(d1.n_segs, next1 + per1);
+            const int q0 = next1 * d1.seg_pairs, q1 = std::min(np1, se * d1.seg_pairs);
+            if (done0 < d1.h && 2 * q1 + 2 * LAT > done0) break;
+            LevelDesc d = d1;
+            d.seg_base = next1;
+            d.n_segs = se - next1;
+            cudaError_t e = launch_level(d, wavelet, false, s, c.d_err);
+            int ev = 0;
+            if (e == cudaSuccess) e = R.record(s, ev);
             if (e != cudaSuccess) return e;
+            emit(1, q0, q1, ev);
+            next1 = se;
         }
-        pending.erase(pending.begin(), pending.begin() + k);
         return cudaSuccess;
     };
-    for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
-        const int se = std::min(nsegs, sb + per_band);
-        const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
-        const int need = std::min(H, 2 * k1 + 2 * LAT);
-        if (need > rows_in) {
-            CK(cudaMemcpy2DAsync(in.f() + rows_in * P, P * 4, host + rows_in * sx, sx, size_t(W) * 4, need - rows_in,
-                                 cudaMemcpyHostToDevice, si));
-            rows_in = need;
-        }
-        CK(cudaEventRecord(c.ev[0][b], si));
-        last_in_ev = b;
-        CK(cudaStreamWaitEvent(s, c.ev[0][b], 0));
+    for (int sb = 0; sb < d0.n_segs; sb += per0) {
+        const int se = std::min(d0.n_segs, sb + per0);
+        const int k0 = sb * d0.seg_pairs, k1 = std::min(np0, se * d0.seg_pairs);
+        // the band's input rows with the warm-up, then the host rows its LH
+        // and HH rows overwrite
+        CK(R.read(2 * k0 - 2 * LAT, 2 * k1 + 2 * LAT));
+        CK(R.read(hd0 + k0, hd0 + std::min(k1, hh0)));
+        CK(R.wait_rows(s, 2 * k0 - 2 * LAT, 2 * k1 + 2 * LAT));
         LevelDesc d = d0;
         d.seg_base = sb;
         d.n_segs = se - sb;
         CK(launch_level(d, wavelet, false, s, c.d_err));
-        CK(cudaEventRecord(c.ev[1][b], s));
-        // HL of rows [k0, k1) and LH, HH of rows [hd + k0, hd + k1)
-        if (W > wd) pending.push_back({k0, k1, wd, W, out.f() + k0 * P + wd, b});
-        const int hk1 = std::min(k1, hh);
-        if (hk1 > k0) pending.push_back({hd + k0, hd + hk1, 0, W, out.f() + (hd + k0) * P, b});
-        std::stable_sort(pending.begin(), pending.end(),
-                         [](const HostOut &x, const HostOut &y) { return x.r1 < y.r1; });
-        CK(flush(false));
+        int ev = 0;
+        CK(R.record(s, ev));
+        emit(0, k0, k1, ev);
+        CK(run_level1(k1));
+        CK(R.flush(false));
     }
-    CK(flush(true));
-    if (J > 1) CK(dense_forward_levels(in.f(), P, out.f(), P, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
-    CK(cudaEventRecord(c.ev[1][63], s));
-    CK(cudaStreamWaitEvent(so, c.ev[1][63], 0));
-    CK(cudaMemcpy2DAsync(host, sx, out.f(), P * 4, size_t(wd) * 4, hd, cudaMemcpyDeviceToHost, so));
+    CK(run_level1(np0));
+    CK(R.flush(true));
+    if (J > 2) {
+        // levels 2 .. J-1 on LL2, then its quadrant (every coarser band)
+        CK(dense_forward_levels(in.f(), P, o, P, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
+        int ev = 0;
+        CK(R.record(s, ev));
+        CK(cudaStreamWaitEvent(so, c.event(ev), 0));
+        CK(cudaMemcpy2DAsync(host, sx, o, P * 4, size_t(ceil_div_pow2(W, 2)) * 4, ceil_div_pow2(H, 2),
+                             cudaMemcpyDeviceToHost, so));
+    }
     // buffers go back to the pool on `s`: order `s` after the copy-out
-    CK(cudaEventRecord(c.ev[0][62], so));
-    CK(cudaStreamWaitEvent(s, c.ev[0][62], 0));
+    int evo = 0;
+    CK(R.record(so, evo));
+    CK(cudaStreamWaitEvent(s, c.event(evo), 0));
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));
 }
@@ -419,24 +569,31 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
     float *buf[2];
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
-    CK(cudaEventRecord(c.ev[0][63], s));
-    CK(cudaStreamWaitEvent(si, c.ev[0][63], 0));
-    CK(cudaStreamWaitEvent(so, c.ev[0][63], 0));
+    int n_ev = 0;
+    auto record = [&](cudaStream_t st) -> cudaEvent_t {
+        cudaEvent_t e = c.event(n_ev++);
+        return e && cudaEventRecord(e, st) == cudaSuccess ? e : nullptr;
+    };
+    cudaEvent_t e0 = record(s);
+    if (!e0) return set_error(DWT_GPU_ECUDA);
+    CK(cudaStreamWaitEvent(si, e0, 0));
+    CK(cudaStreamWaitEvent(so, e0, 0));
 
     const int LAT = wavelet == CDF97 ? 2 : 1;
     const int ws = (W + 1) / 2, hs = (H + 1) / 2, hh = H / 2;
     // the top-left quadrant first: LL1 and every coarser band
     CK(cudaMemcpy2DAsync(in.f(), P * 4, host, sx, size_t(ws) * 4, hs, cudaMemcpyHostToDevice, si));
-    CK(cudaEventRecord(c.ev[0][0], si));
-    CK(cudaStreamWaitEvent(s, c.ev[0][0], 0));
+    cudaEvent_t eq = record(si);
+    if (!eq) return set_error(DWT_GPU_ECUDA);
+    CK(cudaStreamWaitEvent(s, eq, 0));
     if (J > 1) CK(dense_inverse_levels(in.f(), P, out.f(), P, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
 
     LevelDesc d1 = inv_desc(in.f(), P, out.f(), P, W, H, J, 1, buf, p);
     plan_level(d1, 0, true);
     const int npairs = (H + 1) / 2, seg = d1.seg_pairs, nsegs = d1.n_segs;
-    const int per_band = std::max(1, (nsegs + kBands - 1) / kBands);
-    int top_in = 0, bot_in = 0, b = 1;
-    for (int sb = 0; sb < nsegs; sb += per_band, ++b) {
+    const int per_band = std::max(1, (nsegs + kInvBands - 1) / kInvBands);
+    int top_in = 0, bot_in = 0;
+    for (int sb = 0; sb < nsegs; sb += per_band) {
         const int se = std::min(nsegs, sb + per_band);
         const int k0 = sb * seg, k1 = std::min(npairs, se * seg);
         const int r0 = 2 * k0, r1 = std::min(H, 2 * k1);
@@ -453,21 +610,24 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
                                  need_bot - bot_in, cudaMemcpyHostToDevice, si));
         top_in = std::max(top_in, need_top);
         bot_in = std::max(bot_in, need_bot);
-        CK(cudaEventRecord(c.ev[0][b], si));
-        CK(cudaStreamWaitEvent(s, c.ev[0][b], 0));
+        cudaEvent_t ein = record(si);
+        if (!ein) return set_error(DWT_GPU_ECUDA);
+        CK(cudaStreamWaitEvent(s, ein, 0));
         LevelDesc d = d1;
         d.seg_base = sb;
         d.n_segs = se - sb;
         CK(launch_level(d, wavelet, true, s, c.d_err));
-        CK(cudaEventRecord(c.ev[1][b], s));
+        cudaEvent_t eb = record(s);
+        if (!eb) return set_error(DWT_GPU_ECUDA);
         // the output rows overwrite host rows whose input is already read
-        CK(cudaStreamWaitEvent(so, c.ev[1][b], 0));
-        CK(cudaStreamWaitEvent(so, c.ev[0][b], 0));
+        CK(cudaStreamWaitEvent(so, eb, 0));
+        CK(cudaStreamWaitEvent(so, ein, 0));
         CK(cudaMemcpy2DAsync(host + r0 * sx, sx, out.f() + r0 * P, P * 4, size_t(W) * 4, r1 - r0,
                              cudaMemcpyDeviceToHost, so));
     }
-    CK(cudaEventRecord(c.ev[0][62], so));
-    CK(cudaStreamWaitEvent(s, c.ev[0][62], 0));
+    cudaEvent_t eo = record(so);
+    if (!eo) return set_error(DWT_GPU_ECUDA);
+    CK(cudaStreamWaitEvent(s, eo, 0));
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));
 }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <vector>
 
 #include "dwt_pool.h"
 
@@ -18,10 +19,22 @@ struct Context {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t s_in = nullptr, s_out = nullptr;  // copy streams of the pipelined host path
-    cudaEvent_t ev[2][64] = {};                      // band events of the pipelined host path
+    std::vector<cudaEvent_t> events;                 // copy and band events of the pipelined host path
     int *d_err = nullptr;
     Pool pool;
     std::mutex call_mu;  // drop-in calls share `stream`
+
+    // Event i of the pool (created on first use; timing disabled).  Callers
+    // hold call_mu.
+    cudaEvent_t event(size_t i)
+    {
+        while (events.size() <= i) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+            events.push_back(e);
+        }
+        return events[i];
+    }
 };
 
 Context &ctx();

@@ -158,10 +158,11 @@ def test_large_host_frames_pipelined(D, torch):
     """Host frames of 4 Mpx and more take the banded copy/compute pipeline;
     outputs stay bit-identical to the oracle (pinned and pageable memory)."""
     rng = np.random.default_rng(17)
-    for (w, h, pinned) in [(2500, 2000, True), (2049, 2051, False), (4096, 1024, True)]:
+    for (w, h, pinned) in [(2500, 2000, True), (2049, 2051, False), (4096, 1024, True), (8192, 601, True),
+                           (1031, 4099, True)]:
         img = rng.integers(0, 256, size=(h, w)).astype(np.float32)
         for wav in ("cdf97", "cdf53"):
-            for j in (-1, 1, 3):
+            for j in (-1, 1, 2, 3):
                 ref_f, jr = O.transform2_dense(img, wav, "f", j, 0, "s", O.max_threads())
                 ref_i, _ = O.transform2_dense(ref_f, wav, "i", jr, 0, "s", O.max_threads())
                 buf = torch.from_numpy(img.copy())
