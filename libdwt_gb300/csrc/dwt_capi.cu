@@ -175,11 +175,27 @@ size_t dense_scratch_floats(int W, int H, int J, long long *pitch0, long long *p
     return n;
 }
 
+// Largest band (pixels) handed to the single-CTA coarse kernel: a 128 x 128
+// band already runs faster as one more level on the whole GPU (16384^2 CDF
+// 9/7 forward, full depth: 508 us with the coarse kernel from 64 x 64 on,
+// 512-518 us from 128 x 128).
+static long long coarse_max_pixels()
+{
+    static const long long n = [] {
+        const char *e = getenv("DWT_GPU_COARSE_PX");
+        const long long v = e ? atoll(e) : 0;
+        return v > 0 ? v : 4096;
+    }();
+    return n;
+}
+
 // First level whose LL band fits the single-CTA coarse kernel (J if none).
 static int coarse_level(int W, int H, int J)
 {
-    for (int j = 0; j < J; ++j)
-        if (coarse_fits(ceil_div_pow2(W, j), ceil_div_pow2(H, j))) return j;
+    for (int j = 0; j < J; ++j) {
+        const int w = ceil_div_pow2(W, j), h = ceil_div_pow2(H, j);
+        if (coarse_fits(w, h) && (long long)w * h <= coarse_max_pixels()) return j;
+    }
     return J;
 }
 
