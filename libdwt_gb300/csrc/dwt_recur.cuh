@@ -261,10 +261,11 @@ __device__ __forceinline__ void window_inverse(const float *x, int xs, int n, fl
 
 // One pass over `nl` lines of length n, line l at src + l*ls (sample stride
 // xs) into dst + l*ds (stride ys), by threads tid of nthreads, one window
-// (line, segment of kSegPairs output pairs) per item; consecutive threads
-// take consecutive lines.  A line of length 1 is only scaled (the
-// reference's one-sample transform).
-template <int NS, bool INV>
+// (line, segment of SEG output pairs) per item; consecutive threads take
+// consecutive lines.  Long windows do less halo work, short ones have
+// shorter dependency chains per thread.  A line of length 1 is only scaled
+// (the reference's one-sample transform).
+template <int NS, bool INV, int SEG = kSegPairs>
 __device__ __forceinline__ void pass(const float *src, int ls, int xs, float *dst, int ds, int ys, int nl, int n,
                                      const Wavelet &W, int tid, int nthreads)
 {
@@ -273,14 +274,14 @@ __device__ __forceinline__ void pass(const float *src, int ls, int xs, float *ds
         for (int l = tid; l < nl; l += nthreads) dst[l * ds] = fmul(src[l * ls], z);
         return;
     }
-    const int nsegs = ((n + 1) / 2 + kSegPairs - 1) / kSegPairs;
+    const int nsegs = ((n + 1) / 2 + SEG - 1) / SEG;
     const int items = nl * nsegs;
     for (int t = tid; t < items; t += nthreads) {
         const int sgi = t / nl, l = t - sgi * nl;
         if (INV)
-            window_inverse<NS, kSegPairs>(src + l * ls, xs, n, dst + l * ds, ys, sgi * kSegPairs, W);
+            window_inverse<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W);
         else
-            window_forward<NS, kSegPairs>(src + l * ls, xs, n, dst + l * ds, ys, sgi * kSegPairs, W);
+            window_forward<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W);
     }
 }
 
@@ -322,7 +323,7 @@ __device__ __forceinline__ void copy_rect(const float *src, long long sp, float 
 // reference's order); after each level its three detail bands are copied to
 // `out` and the LL band stays in the top-left of A.  Ends with the final LL
 // copied to `out`.  `sync` is the barrier of the participating threads.
-template <int NS, typename Sync>
+template <int NS, int SEG = kSegPairs, typename Sync>
 __device__ __forceinline__ void band_forward(float *A, float *B, int w0, int h0, int levels, float *out,
                                              long long out_pitch, const Wavelet &W, int tid, int nthreads,
                                              Sync sync)
@@ -331,9 +332,9 @@ __device__ __forceinline__ void band_forward(float *A, float *B, int w0, int h0,
     int w = w0, h = h0;
     for (int lvl = 0; lvl < levels; ++lvl) {
         const int wd = (w + 1) >> 1, hd = (h + 1) >> 1;
-        pass<NS, false>(A, P, 1, B, P, 1, h, w, W, tid, nthreads);  // rows
+        pass<NS, false, SEG>(A, P, 1, B, P, 1, h, w, W, tid, nthreads);  // rows
         sync();
-        pass<NS, false>(B, 1, P, A, 1, P, w, h, W, tid, nthreads);  // columns
+        pass<NS, false, SEG>(B, 1, P, A, 1, P, w, h, W, tid, nthreads);  // columns
         sync();
         // detail bands: the w x h region outside [0,hd) x [0,wd)
         copy_rect(A, P, out, out_pitch, wd, w, 0, hd, tid, nthreads);
@@ -347,7 +348,7 @@ __device__ __forceinline__ void band_forward(float *A, float *B, int w0, int h0,
 // All `levels` inverse levels of the coefficient region held in A (the
 // w0 x h0 top-left of a frame in the reference layout): per level, from the
 // coarsest, rows then columns; the rebuilt band ends in A.
-template <int NS, typename Sync>
+template <int NS, int SEG = kSegPairs, typename Sync>
 __device__ __forceinline__ void band_inverse(float *A, float *B, int w0, int h0, int levels, const Wavelet &W,
                                              int tid, int nthreads, Sync sync)
 {
@@ -358,9 +359,9 @@ __device__ __forceinline__ void band_inverse(float *A, float *B, int w0, int h0,
             w = (w + 1) >> 1;
             h = (h + 1) >> 1;
         }
-        pass<NS, true>(A, P, 1, B, P, 1, h, w, W, tid, nthreads);  // rows
+        pass<NS, true, SEG>(A, P, 1, B, P, 1, h, w, W, tid, nthreads);  // rows
         sync();
-        pass<NS, true>(B, 1, P, A, 1, P, w, h, W, tid, nthreads);  // columns
+        pass<NS, true, SEG>(B, 1, P, A, 1, P, w, h, W, tid, nthreads);  // columns
         sync();
     }
 }
