@@ -11,7 +11,9 @@ Printed JSON line (rank 0):
              out of place, CUDA events on the launching stream);
   e2e        the same metric through the drop-in C ABI (dwt_cdf97_2f_s /
              dwt_cdf97_2i_s) on a pinned host image: every step copies the
-             image to the device and the coefficients / reconstruction back;
+             image to the device and the coefficients / reconstruction back
+             (extras.e2e_pageable_16384_mpx_s: the same on a pageable,
+             malloc'ed image, as the reference's callers allocate it);
   roofline   the dominant kernel (level 0 of the forward transform) timed
              alone: algorithmic bytes (read + write, 8 B per pixel) over its
              average duration, against the measured HBM copy peak;
@@ -508,6 +510,18 @@ def run_extras(D, torch, stream, sptr, checks: dict):
         j = D.dwt_cdf97_2f_s(small.ctypes.data, 4096, 4, 1024, 1024, 1024, 1024, 5)
         D.dwt_cdf97_2i_s(small.ctypes.data, 4096, 4, 1024, 1024, 1024, 1024, j)
     out["c0_1024_fwd_inv_host_ms"] = round((time.perf_counter() - t) / n * 1e3, 3)
+    # the drop-in on a pageable (malloc'ed) 16384^2 host image, as the
+    # reference's callers allocate it: forward + inverse, 3 steps after one
+    page = synth.image(16384, 16384, seed=3)
+    pp = page.ctypes.data
+    j = D.dwt_cdf97_2f_s(pp, 16384 * 4, 4, 16384, 16384, 16384, 16384, -1)
+    D.dwt_cdf97_2i_s(pp, 16384 * 4, 4, 16384, 16384, 16384, 16384, j)
+    t = time.perf_counter()
+    for _ in range(3):
+        j = D.dwt_cdf97_2f_s(pp, 16384 * 4, 4, 16384, 16384, 16384, 16384, -1)
+        D.dwt_cdf97_2i_s(pp, 16384 * 4, 4, 16384, 16384, 16384, 16384, j)
+    out["e2e_pageable_16384_mpx_s"] = round(3 * 2 * 16384 * 16384 / (time.perf_counter() - t) / 1e6, 1)
+    del page
     dsmall = torch.from_numpy(small).cuda()
 
     def c0dev():

@@ -67,8 +67,13 @@ Context &ctx()
         c->device = dev ? atoi(dev) : 0;
         cudaSetDevice(c->device);
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-        cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking);
-        cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking);
+        // the copy streams run at the highest priority: where copies are
+        // kernels (host memory the GPU addresses itself) their blocks go
+        // ahead of the band kernels' queued blocks
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        cudaStreamCreateWithPriority(&c->s_in, cudaStreamNonBlocking, greatest);
+        cudaStreamCreateWithPriority(&c->s_out, cudaStreamNonBlocking, greatest);
         cudaMalloc(&c->d_err, sizeof(int));
         cudaMemset(c->d_err, 0, sizeof(int));
         cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
@@ -350,6 +355,38 @@ static int host_bands()
     return n;
 }
 
+// Whether the GPU addresses pageable host memory itself through the host's
+// page tables (address translation services, as on Grace-Blackwell).  Copies
+// to and from pageable memory through the copy engines return only when
+// done (device to host), which would stall the banded pipeline's host
+// thread; a copy kernel stays asynchronous.  DWT_GPU_DIRECT_HOST=0 turns
+// this off.
+static bool pageable_direct()
+{
+    static const bool on = [] {
+        int dev = 0, a = 0, b = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        const char *e = getenv("DWT_GPU_DIRECT_HOST");
+        return a == 1 && b == 1 && !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// A copy of `rows` rows of `width` bytes between host and device memory: a
+// copy kernel when the GPU addresses the host side directly (`kernel`), else
+// the copy engines.
+static cudaError_t copy_rows(bool kernel, void *dst, long long dpitch, const void *src, long long spitch,
+                             long long width, long long rows, cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (kernel) return launch_copy_rows(dst, dpitch, src, spitch, width, rows, s);
+    return cudaMemcpy2DAsync(dst, size_t(dpitch), src, size_t(spitch), size_t(width), size_t(rows), kind, s);
+}
+
 // Host rows of the caller's frame: which copy in read each row (columns
 // [0, split) and [split, W) separately), and the copies out waiting for
 // their rows.  Copy and band events come from the context's pool in order.
@@ -361,6 +398,7 @@ struct HostRows {
     float *dev;
     long long P;
     int W, H, split;
+    bool direct;  // copies by kernel (host memory the GPU addresses itself)
     int n_ev = 0;
     std::vector<int> ev_of[2];  // pool index of the copy that read row r (per column part), -1: unread
     struct Out {
@@ -370,8 +408,10 @@ struct HostRows {
     };
     std::vector<Out> pending;
 
-    HostRows(Context &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_)
-        : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), split(split_)
+    HostRows(Context &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_,
+             bool direct_)
+        : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), split(split_),
+          direct(direct_)
     {
         ev_of[0].assign(H, -1);
         ev_of[1].assign(H, -1);
@@ -402,8 +442,8 @@ struct HostRows {
             while (e < r1 && miss(e) == m) ++e;
             if (m) {
                 const int cb = (m & 1) ? 0 : split, ce = (m & 2) ? W : split;
-                cudaError_t err = cudaMemcpy2DAsync(dev + r * P + cb, P * 4, host + r * sx + cb * 4LL, sx,
-                                                    size_t(ce - cb) * 4, e - r, cudaMemcpyHostToDevice, si);
+                cudaError_t err = copy_rows(direct, dev + r * P + cb, P * 4, host + r * sx + cb * 4LL, sx,
+                                            (ce - cb) * 4LL, e - r, cudaMemcpyHostToDevice, si);
                 int idx = 0;
                 if (err == cudaSuccess) err = record(si, idx);
                 if (err != cudaSuccess) return err;
@@ -464,8 +504,8 @@ struct HostRows {
             cudaError_t e = cudaStreamWaitEvent(so, c.event(o.ev), 0);
             if (e == cudaSuccess && last >= 0) e = cudaStreamWaitEvent(so, c.event(last), 0);
             if (e == cudaSuccess)
-                e = cudaMemcpy2DAsync(host + o.r0 * sx + o.c0 * 4LL, sx, o.src, P * 4, size_t(o.c1 - o.c0) * 4,
-                                      o.r1 - o.r0, cudaMemcpyDeviceToHost, so);
+                e = copy_rows(direct, host + o.r0 * sx + o.c0 * 4LL, sx, o.src, P * 4, (o.c1 - o.c0) * 4LL,
+                              o.r1 - o.r0, cudaMemcpyDeviceToHost, so);
             if (e != cudaSuccess) return e;
         }
         pending.resize(keep);
@@ -473,7 +513,7 @@ struct HostRows {
     }
 };
 
-static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
+static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
 {
     cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
     const long long P = align_up(W, 32);
@@ -485,7 +525,7 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     float *buf[2];
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
-    HostRows R(c, host, sx, in.f(), P, W, H, W);
+    HostRows R(c, host, sx, in.f(), P, W, H, W, direct);
     // the pool may hand out blocks last used on `s`: let the copy streams wait
     int ev0 = 0;
     CK(R.record(s, ev0));
@@ -562,8 +602,8 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
         int ev = 0;
         CK(R.record(s, ev));
         CK(cudaStreamWaitEvent(so, c.event(ev), 0));
-        CK(cudaMemcpy2DAsync(host, sx, o, P * 4, size_t(ceil_div_pow2(W, 2)) * 4, ceil_div_pow2(H, 2),
-                             cudaMemcpyDeviceToHost, so));
+        CK(copy_rows(direct, host, sx, o, P * 4, ceil_div_pow2(W, 2) * 4LL, ceil_div_pow2(H, 2),
+                     cudaMemcpyDeviceToHost, so));
     }
     // buffers go back to the pool on `s`: order `s` after the copy-out
     int evo = 0;
@@ -573,7 +613,7 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     return set_error(check_device_error(c));
 }
 
-static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, int W, int H, int J)
+static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
 {
     cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
     const long long P = align_up(W, 32);
@@ -598,7 +638,7 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
     const int LAT = wavelet == CDF97 ? 2 : 1;
     const int ws = (W + 1) / 2, hs = (H + 1) / 2, hh = H / 2;
     // the top-left quadrant first: LL1 and every coarser band
-    CK(cudaMemcpy2DAsync(in.f(), P * 4, host, sx, size_t(ws) * 4, hs, cudaMemcpyHostToDevice, si));
+    CK(copy_rows(direct, in.f(), P * 4, host, sx, ws * 4LL, hs, cudaMemcpyHostToDevice, si));
     cudaEvent_t eq = record(si);
     if (!eq) return set_error(DWT_GPU_ECUDA);
     CK(cudaStreamWaitEvent(s, eq, 0));
@@ -619,11 +659,11 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
         need_top = std::max(need_top, std::min(hs, r1));
         need_bot = std::max(need_bot, std::min(hh, r1 - hs));
         if (need_top > top_in && W > ws)
-            CK(cudaMemcpy2DAsync(in.f() + top_in * P + ws, P * 4, host + top_in * sx + ws * 4LL, sx,
-                                 size_t(W - ws) * 4, need_top - top_in, cudaMemcpyHostToDevice, si));
+            CK(copy_rows(direct, in.f() + top_in * P + ws, P * 4, host + top_in * sx + ws * 4LL, sx,
+                         (W - ws) * 4LL, need_top - top_in, cudaMemcpyHostToDevice, si));
         if (need_bot > bot_in)
-            CK(cudaMemcpy2DAsync(in.f() + (hs + bot_in) * P, P * 4, host + (hs + bot_in) * sx, sx, size_t(W) * 4,
-                                 need_bot - bot_in, cudaMemcpyHostToDevice, si));
+            CK(copy_rows(direct, in.f() + (hs + bot_in) * P, P * 4, host + (hs + bot_in) * sx, sx, W * 4LL,
+                         need_bot - bot_in, cudaMemcpyHostToDevice, si));
         top_in = std::max(top_in, need_top);
         bot_in = std::max(bot_in, need_bot);
         cudaEvent_t ein = record(si);
@@ -638,8 +678,8 @@ static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, 
         // the output rows overwrite host rows whose input is already read
         CK(cudaStreamWaitEvent(so, eb, 0));
         CK(cudaStreamWaitEvent(so, ein, 0));
-        CK(cudaMemcpy2DAsync(host + r0 * sx, sx, out.f() + r0 * P, P * 4, size_t(W) * 4, r1 - r0,
-                             cudaMemcpyDeviceToHost, so));
+        CK(copy_rows(direct, host + r0 * sx, sx, out.f() + r0 * P, P * 4, W * 4LL, r1 - r0, cudaMemcpyDeviceToHost,
+                     so));
     }
     cudaEvent_t eo = record(so);
     if (!eo) return set_error(DWT_GPU_ECUDA);
@@ -709,6 +749,8 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     cudaStream_t s = c.stream;
     const MemKind kind = classify(ptr);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
+    // pageable host memory the kernels address themselves
+    const bool host_direct = kind == MemKind::Pageable && pageable_direct();
     const bool dense = (ix == ox && iy == oy);
     const long long P = align_up(ox, 32);  // compact pitch in floats
     // a single-row frame may carry any row stride; 2D copies want pitch >= width
@@ -718,8 +760,8 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     {
         const bool rows4h = sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
         if (!on_device && dense && rows4h && (long long)ox * oy >= kPipelineMinPixels && oy >= 64) {
-            return inverse ? pipelined_inverse(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J)
-                           : pipelined_forward(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J);
+            return inverse ? pipelined_inverse(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J, host_direct)
+                           : pipelined_forward(c, wavelet, static_cast<char *>(ptr), csx, ox, oy, J, host_direct);
         }
     }
 
@@ -731,7 +773,12 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     // 2D copies take rows of whole, 4-byte aligned floats; anything else goes
     // through a byte span and the repack kernel
     const bool rows4 = sy == 4 && (csx % 4) == 0 && (reinterpret_cast<uintptr_t>(ptr) & 3) == 0;
-    if (!on_device) {
+    if (host_direct) {
+        if (rows4)
+            CK(launch_copy_rows(in.p, P * 4, ptr, csx, ox * 4LL, oy, s));
+        else
+            CK(launch_repack(ptr, sx, sy, ox, oy, in.f(), P, s));
+    } else if (!on_device) {
         if (rows4) {
             CK(cudaMemcpy2DAsync(in.p, P * 4, ptr, csx, size_t(ox) * 4, oy, cudaMemcpyHostToDevice, s));
         } else {
@@ -792,7 +839,12 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     }
 
     // 3. write back
-    if (!on_device) {
+    if (host_direct) {
+        if (rows4)
+            CK(launch_copy_rows(ptr, csx, out, out_pitch * 4, ox * 4LL, oy, s));
+        else
+            CK(launch_unpack(out, out_pitch, ptr, sx, sy, ox, oy, s));
+    } else if (!on_device) {
         if (rows4) {
             CK(cudaMemcpy2DAsync(ptr, csx, out, out_pitch * 4, size_t(ox) * 4, oy, cudaMemcpyDeviceToHost, s));
         } else {

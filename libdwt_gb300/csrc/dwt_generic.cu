@@ -9,6 +9,10 @@
 //     padding (src/libdwt.c:6377-6397, 6729-6745).
 #include "dwt_generic.cuh"
 
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+
 namespace dwt {
 
 namespace {
@@ -52,6 +56,30 @@ __global__ void unpack_kernel(const float *src, long long spitch, unsigned char 
          k += (long long)gridDim.x * blockDim.x) {
         const int y = int(k / ox), x = int(k % ox);
         store_any(dst + y * sx + x * sy, src[y * spitch + x]);
+    }
+}
+
+// Rows of per_row elements of V from src (pitch spitch bytes) to dst (pitch
+// dpitch bytes): the copy of the host-frame paths where the GPU addresses the
+// caller's host memory itself.  Four independent moves per thread and step
+// keep enough bytes in flight over the host link.
+template <typename V>
+__global__ void copy_rows_kernel(const unsigned char *src, long long spitch, unsigned char *dst, long long dpitch,
+                                 int per_row, int rows)
+{
+    const int step = gridDim.x * blockDim.x;
+    for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+        const V *sr = reinterpret_cast<const V *>(src + r * spitch);
+        V *dr = reinterpret_cast<V *>(dst + r * dpitch);
+        int i = blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * step < per_row; i += 4 * step) {
+            const V a = sr[i], b = sr[i + step], c = sr[i + 2 * step], d = sr[i + 3 * step];
+            dr[i] = a;
+            dr[i + step] = b;
+            dr[i + 2 * step] = c;
+            dr[i + 3 * step] = d;
+        }
+        for (; i < per_row; i += step) dr[i] = sr[i];
     }
 }
 
@@ -217,6 +245,40 @@ cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long lo
     if ((long long)ox * oy == 0) return cudaSuccess;
     unpack_kernel<<<grid_for((long long)ox * oy, 256), 256, 0, s>>>(
         src, spitch, static_cast<unsigned char *>(dst), sx, sy, ox, oy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                             long long rows, cudaStream_t s)
+{
+    if (width <= 0 || rows <= 0) return cudaSuccess;
+    if (rows > INT32_MAX) return cudaErrorInvalidValue;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
+                        uintptr_t(dpitch) | uintptr_t(spitch) | uintptr_t(width);
+    const int vb = (a & 15) == 0 ? 16 : (a & 3) == 0 ? 4 : 1;
+    const long long per_row = width / vb;
+    if (per_row > INT32_MAX) return cudaErrorInvalidValue;
+    // 64 blocks of 256 threads in all (measured best for pageable host frames
+    // of 16384^2 against 32, 128 and 304; DWT_GPU_COPY_CTAS overrides), each
+    // moving 4 x 256 elements of a row per step: enough bytes in flight for
+    // the host link, few blocks to wait for free SM slots among the band
+    // kernels
+    static const int ctas = [] {
+        const char *e = getenv("DWT_GPU_COPY_CTAS");
+        const int v = e ? atoi(e) : 0;
+        return v > 0 ? v : 64;
+    }();
+    const int gx = int(std::min<long long>((per_row + 1023) / 1024, 16));
+    const int gy = int(std::min<long long>(rows, std::max(1, ctas / gx)));
+    const dim3 grid(gx, gy);
+    const auto *sp = static_cast<const unsigned char *>(src);
+    auto *dp = static_cast<unsigned char *>(dst);
+    if (vb == 16)
+        copy_rows_kernel<uint4><<<grid, 256, 0, s>>>(sp, spitch, dp, dpitch, int(per_row), int(rows));
+    else if (vb == 4)
+        copy_rows_kernel<uint32_t><<<grid, 256, 0, s>>>(sp, spitch, dp, dpitch, int(per_row), int(rows));
+    else
+        copy_rows_kernel<unsigned char><<<grid, 256, 0, s>>>(sp, spitch, dp, dpitch, int(per_row), int(rows));
     return cudaGetLastError();
 }
 

@@ -12,6 +12,12 @@ cudaError_t launch_repack(const void *src, long long sx, long long sy, int ox, i
 cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long long sx, long long sy,
                           int ox, int oy, cudaStream_t s);
 
+// `rows` rows of `width` bytes, pitches in bytes, by a kernel: for host
+// memory the GPU addresses directly (pageable memory under address
+// translation services), where it keeps the copy asynchronous to the host.
+cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                             long long rows, cudaStream_t s);
+
 // strided signal bank <-> compact rows (one signal per row)
 // Interleaved channels (pixel = `channels` floats, rows src_pitch_bytes
 // apart) <-> one compact plane per channel (plane c at planes + c *
