@@ -1000,19 +1000,21 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
     Buf in(size_t(P) * 4 + 256, s), out(size_t(P) * 4 + 256, s);
     if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
 
-    // stage the input samples into IN (forward: N samples; inverse: L then H)
+    // stage the input samples into IN (forward: N samples; inverse: L then H);
+    // the gather and scatter kernels address device memory and pageable host
+    // memory the GPU reaches itself, the copy engines the rest
+    auto kernel_reach = [](const void *p) {
+        const MemKind k = classify(p);
+        return k == MemKind::Device || k == MemKind::Managed || (k == MemKind::Pageable && pageable_direct());
+    };
     auto gather = [&](const float *src, float *dst, int n) -> cudaError_t {
         if (n == 0) return cudaSuccess;
-        const MemKind k = classify(src);
-        if (k == MemKind::Device || k == MemKind::Managed)
-            return launch_gather_signals(src, n, stride, 1, 1, 0, 0, dst, P, s);
+        if (kernel_reach(src)) return launch_gather_signals(src, n, stride, 1, 1, 0, 0, dst, P, s);
         return cudaMemcpy2DAsync(dst, 4, src, stride, 4, n, cudaMemcpyHostToDevice, s);
     };
     auto scatter = [&](const float *src, float *dst, int n) -> cudaError_t {
         if (n == 0) return cudaSuccess;
-        const MemKind k = classify(dst);
-        if (k == MemKind::Device || k == MemKind::Managed)
-            return launch_scatter_signals(src, P, n, dst, stride, 1, 1, 0, 0, s);
+        if (kernel_reach(dst)) return launch_scatter_signals(src, P, n, dst, stride, 1, 1, 0, 0, s);
         return cudaMemcpy2DAsync(dst, stride, src, 4, 4, n, cudaMemcpyDeviceToHost, s);
     };
 

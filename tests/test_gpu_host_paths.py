@@ -53,3 +53,43 @@ def test_pageable_host_frames(tmp_path, direct, w, h, sy, wav):
     assert np.array_equal(out["inv"], ref_i)
     if sy > 4:
         assert not out["rest"].any()  # samples between the pixels are untouched
+
+
+CHILD_1D = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import libdwt_gb300 as D
+N, k, wav, src, dst = int(sys.argv[2]), int(sys.argv[3]), sys.argv[4], sys.argv[5], sys.argv[6]
+x = np.load(src)                          # N samples, every k-th float of a host buffer
+buf = np.zeros(N * k + 8, np.float32)
+buf[:N * k:k] = x
+a = buf.copy()
+D.strided_1d(wav, False, a, None, a, a[(N + 1) // 2 * k:], N, 4 * k)   # in place: L then H
+fwd = a.copy()
+D.strided_1d(wav, True, a, a[(N + 1) // 2 * k:], a, None, N, 4 * k)
+np.savez(dst, fwd=fwd, inv=a)
+"""
+
+
+@pytest.mark.parametrize("direct", ["1", "0"])
+@pytest.mark.parametrize("N,k,wav", [(1, 1, "cdf97"), (2, 8, "cdf53"), (7, 3, "cdf97"), (4097, 8, "cdf97"),
+                                     (1000, 1, "cdf53")])
+def test_pageable_1d_signals(tmp_path, direct, N, k, wav):
+    rng = np.random.default_rng(N + k)
+    x = rng.standard_normal(N).astype(np.float32)
+    src, dst = str(tmp_path / "x.npy"), str(tmp_path / "o.npz")
+    np.save(src, x)
+    env = dict(os.environ, DWT_GPU_DIRECT_HOST=direct)
+    r = subprocess.run([sys.executable, "-c", CHILD_1D, ROOT, str(N), str(k), wav, src, dst], capture_output=True,
+                       text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    out = np.load(dst)
+    buf = np.zeros(N * k + 8, np.float32)
+    buf[:N * k:k] = x
+    ref = buf.copy()
+    base = ref.ctypes.data
+    hoff = (N + 1) // 2 * k * 4
+    O.strided_1d(wav, "f", base, base, base + hoff, N, 4 * k)
+    assert np.array_equal(out["fwd"], ref)
+    O.strided_1d(wav, "i", base, base + hoff, base, N, 4 * k)
+    assert np.array_equal(out["inv"], ref)
