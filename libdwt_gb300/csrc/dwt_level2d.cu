@@ -141,13 +141,17 @@ namespace {
 
 // Segment length of a 2D level, measured on the levels of 16384^2 (level
 // kernel times under ncu): the forward is fastest with about 176 segments
-// per level (none shorter than 8 pairs from 1024 row pairs up, 4 below);
-// the inverse with about 88 on large levels and 128 (at least 4 pairs) from
+// per level (none shorter than 8 pairs from 1024 row pairs up, 2 below);
+// the inverse with about 88 on large levels and 128 (at least 2 pairs) from
 // 1024 row pairs down.
 constexpr int kSegsForward = 176;
 constexpr int kSegsInverse = 88;
 constexpr int kSegsInverseSmall = 128;
 constexpr int kSmallPairs = 1024;
+// Below kSmallPairs the levels are latency-bound: segments as short as 2
+// pairs (more, shorter units) measured 5 us faster per 16384^2 forward +
+// inverse than a 4-pair minimum.
+constexpr int kSegMinSmall = 2;
 
 int env_int(const char *name, int dflt)
 {
@@ -173,11 +177,11 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
             static const int segs_f = std::max(1, env_int("DWT_GPU_SEGS_FWD", kSegsForward));
             static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
             if (!inverse)
-                seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : 4);
+                seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : kSegMinSmall);
             else if (npairs > kSmallPairs)
                 seg = std::max(ceil_div(npairs, segs_i), 4);
             else
-                seg = std::max(ceil_div(npairs, kSegsInverseSmall), 4);
+                seg = std::max(ceil_div(npairs, kSegsInverseSmall), kSegMinSmall);
         }
     }
     seg = std::min(seg, std::max(npairs, 1));
