@@ -406,13 +406,10 @@ int batch_smem_bytes() { return kBatchWarps * (kStages * kStageFloats * 4 + kSta
 cudaError_t launch_batch_kernel(int grid, const BatchImage *imgs, const BatchItem *items, int n_items,
                                 int *counters, int *err, cudaStream_t s)
 {
-    static bool configured = false;
-    if (!configured) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem_bytes());
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // once per process, safe from several host threads
+    static const cudaError_t configured =
+        cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem_bytes());
+    if (configured != cudaSuccess) return configured;
     batch_kernel<<<grid, kBatchWarps * 32, batch_smem_bytes(), s>>>(imgs, items, n_items, counters, counters + 1, err);
     return cudaGetLastError();
 }

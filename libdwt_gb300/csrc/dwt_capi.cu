@@ -20,6 +20,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/libdwt.h"
@@ -67,16 +68,23 @@ Context &ctx()
         c->device = dev ? atoi(dev) : 0;
         cudaSetDevice(c->device);
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        cudaMalloc(&c->d_err, sizeof(int));
+        cudaMemset(c->d_err, 0, sizeof(int));
+        cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
         // the copy streams run at the highest priority: where copies are
         // kernels (host memory the GPU addresses itself) their blocks go
         // ahead of the band kernels' queued blocks
         int least = 0, greatest = 0;
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
-        cudaStreamCreateWithPriority(&c->s_in, cudaStreamNonBlocking, greatest);
-        cudaStreamCreateWithPriority(&c->s_out, cudaStreamNonBlocking, greatest);
-        cudaMalloc(&c->d_err, sizeof(int));
-        cudaMemset(c->d_err, 0, sizeof(int));
-        cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+        for (Lane &l : c->lanes) {
+            l.sm_count = c->sm_count;
+            cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking);
+            cudaStreamCreateWithPriority(&l.s_in, cudaStreamNonBlocking, greatest);
+            cudaStreamCreateWithPriority(&l.s_out, cudaStreamNonBlocking, greatest);
+            cudaMalloc(&l.d_err, sizeof(int));
+            cudaMemset(l.d_err, 0, sizeof(int));
+        }
+        cudaDeviceSynchronize();
         g_ctx = c;
     }
     cudaSetDevice(g_ctx->device);
@@ -88,14 +96,33 @@ void ctx_finish()
     std::lock_guard<std::mutex> g(g_init_mu);
     if (!g_ctx) return;
     cudaStreamSynchronize(g_ctx->stream);
+    for (Lane &l : g_ctx->lanes) {
+        std::lock_guard<std::mutex> lg(l.mu);
+        cudaStreamSynchronize(l.stream);
+    }
     g_ctx->pool.release_all();
     cudaFree(g_ctx->d_err);
-    for (cudaEvent_t e : g_ctx->events) cudaEventDestroy(e);
-    cudaStreamDestroy(g_ctx->s_in);
-    cudaStreamDestroy(g_ctx->s_out);
+    for (Lane &l : g_ctx->lanes) {
+        for (cudaEvent_t e : l.events) cudaEventDestroy(e);
+        cudaStreamDestroy(l.s_in);
+        cudaStreamDestroy(l.s_out);
+        cudaStreamDestroy(l.stream);
+        cudaFree(l.d_err);
+    }
     cudaStreamDestroy(g_ctx->stream);
     delete g_ctx;
     g_ctx = nullptr;
+}
+
+LaneGuard::LaneGuard(Context &c)
+{
+    for (Lane &l : c.lanes)
+        if (l.mu.try_lock()) {
+            lane_ = &l;
+            return;
+        }
+    lane_ = &c.lanes[std::hash<std::thread::id>{}(std::this_thread::get_id()) % kCallLanes];
+    lane_->mu.lock();
 }
 
 // ------------------------------------------------------------ helpers
@@ -154,18 +181,20 @@ struct Buf {
         }                                                                      \
     } while (0)
 
-// Reads and clears the device error word after the stream drained.
-static int check_device_error(Context &c)
+// Reads and clears a device error word after its stream drained.
+static int check_device_error(int *d_err)
 {
     int h = 0;
-    if (cudaMemcpy(&h, c.d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DWT_GPU_ECUDA;
+    if (cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DWT_GPU_ECUDA;
     if (h) {
-        cudaMemset(c.d_err, 0, sizeof(int));
+        cudaMemset(d_err, 0, sizeof(int));
         log_error("device-side wait gave up (code %d)\n", h);
         return DWT_GPU_EDEVICE;
     }
     return DWT_GPU_OK;
 }
+static int check_device_error(Context &c) { return check_device_error(c.d_err); }
+static int check_device_error(Lane &l) { return check_device_error(l.d_err); }
 
 // ------------------------------------------------------- level pipelines
 
@@ -391,7 +420,7 @@ static cudaError_t copy_rows(bool kernel, void *dst, long long dpitch, const voi
 // [0, split) and [split, W) separately), and the copies out waiting for
 // their rows.  Copy and band events come from the context's pool in order.
 struct HostRows {
-    Context &c;
+    Lane &c;
     cudaStream_t si, so;
     char *host;
     long long sx;
@@ -408,7 +437,7 @@ struct HostRows {
     };
     std::vector<Out> pending;
 
-    HostRows(Context &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_,
+    HostRows(Lane &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_,
              bool direct_)
         : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), split(split_),
           direct(direct_)
@@ -513,7 +542,7 @@ struct HostRows {
     }
 };
 
-static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
+static int pipelined_forward(Lane &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
 {
     cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
     const long long P = align_up(W, 32);
@@ -613,7 +642,7 @@ static int pipelined_forward(Context &c, int wavelet, char *host, long long sx, 
     return set_error(check_device_error(c));
 }
 
-static int pipelined_inverse(Context &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
+static int pipelined_inverse(Lane &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
 {
     cudaStream_t s = c.stream, si = c.s_in, so = c.s_out;
     const long long P = align_up(W, 32);
@@ -744,8 +773,8 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
         return set_error(DWT_GPU_EINVAL);
     }
 
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const MemKind kind = classify(ptr);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
@@ -884,8 +913,8 @@ static int run_2d_d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox
         log_error("null image pointer\n");
         return set_error(DWT_GPU_EINVAL);
     }
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const MemKind kind = classify(ptr);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
@@ -942,8 +971,8 @@ static int run_1d_d(int wavelet, bool inverse, const double *a, const double *b,
         log_error("stride %d smaller than a sample\n", stride);
         return set_error(DWT_GPU_EINVAL);
     }
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const int nl = (N + 1) / 2, nh = N / 2;
     Buf line(size_t(N) * 8 + 256, s), tmp(size_t(N) * 8 + 256, s);
@@ -992,8 +1021,8 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
         log_error("stride %d smaller than a sample\n", stride);
         return set_error(DWT_GPU_EINVAL);
     }
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const int nl = (N + 1) / 2, nh = N / 2;
     const long long P = align_up(N, 32);
@@ -1064,8 +1093,8 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
     }
     if (N == 0 || count == 0) return DWT_GPU_OK;
     if (count > 0x7fffffffLL) return set_error(DWT_GPU_EINVAL);
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const MemKind kind = classify(base);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;
@@ -1161,8 +1190,8 @@ static int run_2d_channels(int wavelet, bool inverse, void *ptr, int stride_x, i
         J = (*j_levels < 0 || *j_levels > lim) ? lim : *j_levels;
     }
     if (J == 0 || w == 0 || h == 0) return DWT_GPU_OK;
-    Context &c = ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
     const MemKind kind = classify(ptr);
     const bool on_device = kind == MemKind::Device || kind == MemKind::Managed;

@@ -12,20 +12,19 @@ namespace dwt {
 
 enum class MemKind { Pageable, Pinned, Device, Managed };
 
-// One GPU context per process: device, working stream of the drop-in calls,
-// the buffer pool and the device error word.
-struct Context {
-    int device = 0;
+// The streams, events and device error word of one drop-in call at a time.
+// Calls from several host threads take different lanes, so their copies and
+// kernels overlap on the GPU.
+struct Lane {
+    std::mutex mu;
     int sm_count = 0;
-    cudaStream_t stream = nullptr;
-    cudaStream_t s_in = nullptr, s_out = nullptr;  // copy streams of the pipelined host path
+    cudaStream_t stream = nullptr;                  // kernels
+    cudaStream_t s_in = nullptr, s_out = nullptr;  // copies of the pipelined host path
     std::vector<cudaEvent_t> events;                 // copy and band events of the pipelined host path
     int *d_err = nullptr;
-    Pool pool;
-    std::mutex call_mu;  // drop-in calls share `stream`
 
-    // Event i of the pool (created on first use; timing disabled).  Callers
-    // hold call_mu.
+    // Event i of the lane (created on first use; timing disabled).  The
+    // caller holds mu.
     cudaEvent_t event(size_t i)
     {
         while (events.size() <= i) {
@@ -36,9 +35,36 @@ struct Context {
         return events[i];
     }
 };
+constexpr int kCallLanes = 8;
+
+// One GPU context per process: device, the drop-in lanes, the stream and
+// device error word of the batched, serving and device-resident forms, and
+// the buffer pool.
+struct Context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    int *d_err = nullptr;
+    Pool pool;
+    Lane lanes[kCallLanes];
+};
 
 Context &ctx();
 void ctx_finish();
+
+// Holds a drop-in lane for the duration of a call: a free one if any, else
+// the calling thread's own (waiting for it).
+class LaneGuard {
+public:
+    explicit LaneGuard(Context &c);
+    ~LaneGuard() { lane_->mu.unlock(); }
+    LaneGuard(const LaneGuard &) = delete;
+    LaneGuard &operator=(const LaneGuard &) = delete;
+    Lane &get() { return *lane_; }
+
+private:
+    Lane *lane_;
+};
 void log_error(const char *fmt, ...);
 int set_error(int code);
 MemKind classify(const void *p);

@@ -106,15 +106,15 @@ cudaError_t configure(K kernel)
 cudaError_t launch_coarse(bool inverse, const float *in, long long in_pitch, int w, int h, int levels,
                           float *out, long long out_pitch, int wavelet, cudaStream_t s)
 {
-    static bool configured = false;
-    if (!configured) {
+    // once per process, safe from several host threads
+    static const cudaError_t configured = [] {
         cudaError_t e = configure(coarse_forward_kernel<4>);
         if (e == cudaSuccess) e = configure(coarse_inverse_kernel<4>);
         if (e == cudaSuccess) e = configure(coarse_forward_kernel<2>);
         if (e == cudaSuccess) e = configure(coarse_inverse_kernel<2>);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+        return e;
+    }();
+    if (configured != cudaSuccess) return configured;
     if (!coarse_fits(w, h)) return cudaErrorInvalidValue;
     const Wavelet W = make_wavelet(wavelet, inverse);
     const size_t smem = size_t(4) * recur::band_floats(w, h);

@@ -118,13 +118,10 @@ bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M)
 template <int NS, bool INV>
 cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
 {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(level_kernel<NS, INV>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // once per instantiation, safe from several host threads
+    static const cudaError_t configured =
+        cudaFuncSetAttribute(level_kernel<NS, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (configured != cudaSuccess) return configured;
     const int units = d.n_strips * d.n_segs;
     const int grid = ceil_div(units, kWarpsPerCta);
     LevelMaps M;

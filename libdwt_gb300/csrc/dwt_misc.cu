@@ -45,12 +45,12 @@ void zero_strided(void *base, long long stride, int n, int elem)
         }
         return;
     }
-    dwt::Context &c = dwt::ctx();
-    std::lock_guard<std::mutex> g(c.call_mu);
+    dwt::LaneGuard lane(dwt::ctx());
+    const cudaStream_t s = lane.get().stream;
     const int block = 256, grid = (n + block - 1) / block < 1024 ? (n + block - 1) / block : 1024;
-    zero_strided_kernel<<<grid, block, 0, c.stream>>>(static_cast<char *>(base), stride, n, elem);
+    zero_strided_kernel<<<grid, block, 0, s>>>(static_cast<char *>(base), stride, n, elem);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         dwt::log_error("zero padding on device memory failed: %s\n", cudaGetErrorString(e));
         abort();

@@ -76,13 +76,10 @@ cudaError_t launch_t(float *base, int N, int G, long long group_stride_f, long l
                      int sm_count, int *err)
 {
     const size_t smem = size_t(N) * G * 4;
-    static bool configured = false;
-    if (!configured) {
-        const cudaError_t e = cudaFuncSetAttribute(signals_kernel<NS, INV>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSignalsMaxSmem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // once per instantiation, safe from several host threads
+    static const cudaError_t configured =
+        cudaFuncSetAttribute(signals_kernel<NS, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSignalsMaxSmem);
+    if (configured != cudaSuccess) return configured;
     const int per_signal = kSigThreads / G;
     const int npairs = (N + 1) / 2;
     const int seg = (npairs + per_signal - 1) / per_signal;
