@@ -430,6 +430,13 @@ DWT_EXPORT int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const f
                                  const long long in_pitch_bytes[4], float *const out[4],
                                  const long long out_pitch_bytes[4], void *stream);
 
+/* Failure detection without a fault: a one-warp kernel waits on an mbarrier
+ * that nothing completes, through the same bounded wait the level kernels
+ * use, limited to `iterations` tries.  The wait gives up, sets the device
+ * error word and returns; the call reports DWT_GPU_EDEVICE (and logs the
+ * code), and the context stays usable.  DWT_GPU_EINVAL for iterations <= 0. */
+DWT_EXPORT int dwt_gpu_selftest_wait_timeout(int iterations);
+
 /* Waits for all device work and reports (and clears) a device-side error. */
 DWT_EXPORT int dwt_gpu_sync_check(void);
 

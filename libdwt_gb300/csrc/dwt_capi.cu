@@ -1266,6 +1266,22 @@ int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_
     return J;
 }
 
+// Failure detection, exercised without a fault: one warp waits on an
+// mbarrier that nothing completes, through the bounded wait the level kernels
+// use, with a short limit.  The wait gives up, the error word is set and the
+// kernel returns normally.
+__global__ void wait_timeout_kernel(uint32_t iterations, int *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const bool done = mbar_wait_bounded(&bar, 0, iterations);  // no arrival is ever made
+    if (!__all_sync(0xffffffffu, done) && threadIdx.x == 0) atomicCAS(err, 0, int(kErrWaitTimeout));
+}
+
 }  // namespace dwt
 
 using namespace dwt;
@@ -1396,6 +1412,18 @@ int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const float *const
         return set_error(DWT_GPU_ECUDA);
     }
     return DWT_GPU_OK;
+}
+
+int dwt_gpu_selftest_wait_timeout(int iterations)
+{
+    t_last_error = DWT_GPU_OK;
+    if (iterations <= 0) return set_error(DWT_GPU_EINVAL);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
+    wait_timeout_kernel<<<1, 32, 0, c.stream>>>(uint32_t(iterations), c.d_err);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c.stream));
+    return set_error(check_device_error(c));
 }
 
 int dwt_gpu_sync_check(void)

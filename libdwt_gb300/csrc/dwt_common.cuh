@@ -199,9 +199,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 // hardware-chosen interval, so the iteration cap is seconds of wall time.
 constexpr uint32_t kWaitLimit = 1u << 24;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit = kWaitLimit)
 {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
