@@ -416,9 +416,9 @@ static cudaError_t copy_rows(bool kernel, void *dst, long long dpitch, const voi
     return cudaMemcpy2DAsync(dst, size_t(dpitch), src, size_t(spitch), size_t(width), size_t(rows), kind, s);
 }
 
-// Host rows of the caller's frame: which copy in read each row (columns
-// [0, split) and [split, W) separately), and the copies out waiting for
-// their rows.  Copy and band events come from the context's pool in order.
+// Host rows of the caller's frame: which copy in read each row, and the
+// copies out waiting for their rows.  Copy and band events come from the
+// lane's pool in order.
 struct HostRows {
     Lane &c;
     cudaStream_t si, so;
@@ -426,10 +426,10 @@ struct HostRows {
     long long sx;
     float *dev;
     long long P;
-    int W, H, split;
-    bool direct;  // copies by kernel (host memory the GPU addresses itself)
+    int W, H;
+    bool direct;              // copies by kernel (host memory the GPU addresses itself)
     int n_ev = 0;
-    std::vector<int> ev_of[2];  // pool index of the copy that read row r (per column part), -1: unread
+    std::vector<int> ev_of;   // lane event of the copy that read row r, -1 while unread
     struct Out {
         int r0, r1, c0, c1;  // host rows / columns
         const float *src;    // device address of (r0, c0), pitch P
@@ -437,13 +437,10 @@ struct HostRows {
     };
     std::vector<Out> pending;
 
-    HostRows(Lane &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, int split_,
-             bool direct_)
-        : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), split(split_),
-          direct(direct_)
+    HostRows(Lane &c_, char *host_, long long sx_, float *dev_, long long P_, int W_, int H_, bool direct_)
+        : c(c_), si(c_.s_in), so(c_.s_out), host(host_), sx(sx_), dev(dev_), P(P_), W(W_), H(H_), direct(direct_),
+          ev_of(H_, -1)
     {
-        ev_of[0].assign(H, -1);
-        ev_of[1].assign(H, -1);
     }
 
     cudaError_t record(cudaStream_t st, int &idx)
@@ -453,61 +450,46 @@ struct HostRows {
         return e ? cudaEventRecord(e, st) : cudaErrorMemoryAllocation;
     }
 
-    // Copies in every unread part of rows [r0, r1) selected by `parts`
-    // (bit 0: columns [0, split), bit 1: [split, W)); one copy per run of
-    // rows that miss the same parts.
-    cudaError_t read(int r0, int r1, int parts = 3)
+    // Copies in every unread row of [r0, r1), one copy per run of unread rows.
+    cudaError_t read(int r0, int r1)
     {
         r0 = std::max(r0, 0);
         r1 = std::min(r1, H);
-        if (split >= W) parts &= 1;
-        if (split <= 0) parts &= 2;
-        auto miss = [&](int r) {
-            return ((parts & 1) && ev_of[0][r] < 0 ? 1 : 0) | ((parts & 2) && ev_of[1][r] < 0 ? 2 : 0);
-        };
         for (int r = r0; r < r1;) {
-            const int m = miss(r);
-            int e = r + 1;
-            while (e < r1 && miss(e) == m) ++e;
-            if (m) {
-                const int cb = (m & 1) ? 0 : split, ce = (m & 2) ? W : split;
-                cudaError_t err = copy_rows(direct, dev + r * P + cb, P * 4, host + r * sx + cb * 4LL, sx,
-                                            (ce - cb) * 4LL, e - r, cudaMemcpyHostToDevice, si);
-                int idx = 0;
-                if (err == cudaSuccess) err = record(si, idx);
-                if (err != cudaSuccess) return err;
-                for (int k = r; k < e; ++k) {
-                    if (m & 1) ev_of[0][k] = idx;
-                    if (m & 2) ev_of[1][k] = idx;
-                }
+            if (ev_of[r] >= 0) {
+                ++r;
+                continue;
             }
+            int e = r + 1;
+            while (e < r1 && ev_of[e] < 0) ++e;
+            cudaError_t err = copy_rows(direct, dev + r * P, P * 4, host + r * sx, sx, W * 4LL, e - r,
+                                        cudaMemcpyHostToDevice, si);
+            int idx = 0;
+            if (err == cudaSuccess) err = record(si, idx);
+            if (err != cudaSuccess) return err;
+            for (int k = r; k < e; ++k) ev_of[k] = idx;
             r = e;
         }
         return cudaSuccess;
     }
 
-    // Latest copy that read a selected part of rows [r0, r1); -2 if one of
-    // them is unread, -1 if none needed a copy.
-    int last_copy(int r0, int r1, int parts = 3) const
+    // Latest copy that read a row of [r0, r1); -2 if one of them is unread.
+    int last_copy(int r0, int r1) const
     {
         r0 = std::max(r0, 0);
         r1 = std::min(r1, H);
-        if (split >= W) parts &= 1;
-        if (split <= 0) parts &= 2;
         int last = -1;
-        for (int r = r0; r < r1; ++r)
-            for (int q = 0; q < 2; ++q)
-                if (parts & (1 << q)) {
-                    if (ev_of[q][r] < 0) return -2;
-                    last = std::max(last, ev_of[q][r]);
-                }
+        for (int r = r0; r < r1; ++r) {
+            if (ev_of[r] < 0) return -2;
+            last = std::max(last, ev_of[r]);
+        }
         return last;
     }
 
-    // Stream `st` waits until the selected parts of rows [r0, r1) are in.
-    cudaError_t wait_rows(cudaStream_t st, int r0, int r1, int parts = 3)
+    // Stream `st` waits until rows [r0, r1) are in.
+    cudaError_t wait_rows(cudaStream_t st, int r0, int r1)
     {
-        const int last = last_copy(r0, r1, parts);
+        const int last = last_copy(r0, r1);
         if (last == -2) return cudaErrorInvalidValue;  // a scheduling bug: rows not read
         return last >= 0 ? cudaStreamWaitEvent(st, c.event(last), 0) : cudaSuccess;
     }
@@ -554,7 +536,7 @@ static int pipelined_forward(Lane &c, int wavelet, char *host, long long sx, int
     float *buf[2];
     long long p[2];
     scratch_frames(W, H, J, scratch.f(), buf, p);
-    HostRows R(c, host, sx, in.f(), P, W, H, W, direct);
+    HostRows R(c, host, sx, in.f(), P, W, H, direct);
     // the pool may hand out blocks last used on `s`: let the copy streams wait
     int ev0 = 0;
     CK(R.record(s, ev0));
