@@ -132,10 +132,13 @@ DWT_EXPORT void dwt_cdf53_i_d(const double *src, double *dst, double *tmp, int N
 /* ----------------------------------------------------------------- lifecycle */
 
 /* src/libdwt.h:851 (src/libdwt.c:7466-7490): bring up the GPU context, the
- * working stream and the buffer pool (also done lazily by the first call). */
+ * buffer pool and the call lanes (streams, events and device error word of
+ * one call each, so that calls from several host threads overlap); also done
+ * lazily by the first call. */
 DWT_EXPORT void dwt_util_init(void);
 
-/* src/libdwt.h:856 (src/libdwt.c:7492-7510): release the pool and stream. */
+/* src/libdwt.h:856 (src/libdwt.c:7492-7510): release the pool, the lanes and
+ * the context's streams. */
 DWT_EXPORT void dwt_util_finish(void);
 
 /* src/libdwt.h:845 (src/libdwt.c:7668-7672): selects a CPU lifting kernel in
