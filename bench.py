@@ -437,7 +437,7 @@ def main():
                          "launch_ms": round(kms, 4)},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": args.steps * 2 * J,
+            "gpu_launches": args.steps * 2 * D.lib().dwt_gpu_dense_launches(W, H, J),
             "roundtrip_max_abs_err": err_rt,
             "errors_vs_fp64": errors,
             "extras": extras,

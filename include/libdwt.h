@@ -433,6 +433,12 @@ DWT_EXPORT int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const f
                                  const long long in_pitch_bytes[4], float *const out[4],
                                  const long long out_pitch_bytes[4], void *stream);
 
+/* Kernel launches of one dense transform of a w x h image to j_levels
+ * levels (< 0: the full depth of the smaller side), the same in either
+ * direction: one level kernel per level down to the band the single-CTA
+ * coarse kernel takes, then one coarse launch for the rest. */
+DWT_EXPORT int dwt_gpu_dense_launches(int w, int h, int j_levels);
+
 /* Failure detection without a fault: a one-warp kernel waits on an mbarrier
  * that nothing completes, through the same bounded wait the level kernels
  * use, limited to `iterations` tries.  The wait gives up, sets the device

@@ -1396,6 +1396,15 @@ int dwt_gpu_level_dev(int wavelet, int inverse, int w, int h, const float *const
     return DWT_GPU_OK;
 }
 
+int dwt_gpu_dense_launches(int w, int h, int j_levels)
+{
+    if (w <= 0 || h <= 0) return set_error(DWT_GPU_EINVAL);
+    const int J = j_levels < 0 ? ceil_log2_int(std::min(w, h)) : j_levels;
+    if (J == 0) return 0;
+    const int j0 = coarse_level(w, h, J);
+    return j0 + (j0 < J ? 1 : 0);
+}
+
 int dwt_gpu_selftest_wait_timeout(int iterations)
 {
     t_last_error = DWT_GPU_OK;

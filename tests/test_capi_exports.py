@@ -51,3 +51,18 @@ def test_host_helpers(lib):
         assert L.dwt_util_pow2_ceil_log2(x) == 1 << e
     L.dwt_gpu_error_string.restype = ctypes.c_char_p
     assert L.dwt_gpu_error_string(-1) == b"invalid argument"
+
+
+def test_dense_launch_plan(lib):
+    """One level kernel per level down to the coarse kernel's band (at most
+    64 x 64 pixels), then one coarse launch: the count bench.py reports."""
+    L, _ = lib
+    L.dwt_gpu_dense_launches.argtypes = [ctypes.c_int] * 3
+    assert L.dwt_gpu_dense_launches(16384, 16384, 14) == 9   # 16384^2 .. 128^2, then 64^2 .. 1
+    assert L.dwt_gpu_dense_launches(16384, 16384, -1) == 9
+    assert L.dwt_gpu_dense_launches(16383, 16385, 14) == 10  # its 64 x 65 band is above 4096 pixels
+    assert L.dwt_gpu_dense_launches(1024, 1024, 5) == 5
+    assert L.dwt_gpu_dense_launches(64, 64, 6) == 1
+    assert L.dwt_gpu_dense_launches(128, 128, 1) == 1        # one level, no coarse launch
+    assert L.dwt_gpu_dense_launches(8, 8, 0) == 0
+    assert L.dwt_gpu_dense_launches(0, 8, 1) == -1
