@@ -76,3 +76,42 @@ def test_every_size_up_to_40(D):
                 if not frame_equal(got, ref, sx, sy, ox, oy):
                     bad.append((w, h, wav, kind, sx, sy, ox, oy, j, d1, zp, "i"))
     assert not bad, bad[:20]
+
+
+def test_every_size_up_to_40_on_device_with_guard_bands(D):
+    """The same sweep on device frames (dense aligned frames are transformed
+    in place by the level kernels, the rest through the repack and unpack
+    kernels), each frame between 256-byte guard bands that must come back
+    untouched."""
+    import torch
+    G = 256
+    rng = np.random.default_rng(41)
+    bad = []
+    for w in range(1, 41):
+        for h in range(1, 41):
+            for wav in ("cdf97", "cdf53"):
+                kind, sx, sy, ox, oy, j, d1, zp = _case(rng, w, h)
+                nbytes = sx * (oy - 1) + sy * (ox - 1) + 4
+                host = rng.integers(0, 256, size=nbytes + 2 * G).astype(np.uint8)
+                ys, xs = np.meshgrid(np.arange(oy), np.arange(ox), indexing="ij")
+                offs = G + (ys * sx + xs * sy).ravel()
+                vals = rng.integers(0, 256, size=offs.size).astype(np.float32).view(np.uint8).reshape(-1, 4)
+                for b in range(4):
+                    host[offs + b] = vals[:, b]
+                ref = host[G:G + nbytes].copy()
+                dev = torch.from_numpy(host).cuda()
+                frame = dev[G:G + nbytes]
+                jr = O.transform2(ref, wav, "f", sx, sy, (ox, oy), (w, h), j, d1, zp)
+                jg = D.transform2(frame, wav, "f", sx, sy, (ox, oy), (w, h), j, d1, zp)
+                got = dev.cpu().numpy()
+                guards_ok = np.array_equal(got[:G], host[:G]) and np.array_equal(got[G + nbytes:], host[G + nbytes:])
+                if jr != jg or not guards_ok or not frame_equal(got[G:G + nbytes], ref, sx, sy, ox, oy):
+                    bad.append((w, h, wav, kind, sx, sy, ox, oy, j, d1, zp, "f", guards_ok))
+                    continue
+                O.transform2(ref, wav, "i", sx, sy, (ox, oy), (w, h), jr, d1, zp)
+                D.transform2(frame, wav, "i", sx, sy, (ox, oy), (w, h), jr, d1, zp)
+                got = dev.cpu().numpy()
+                guards_ok = np.array_equal(got[:G], host[:G]) and np.array_equal(got[G + nbytes:], host[G + nbytes:])
+                if not guards_ok or not frame_equal(got[G:G + nbytes], ref, sx, sy, ox, oy):
+                    bad.append((w, h, wav, kind, sx, sy, ox, oy, j, d1, zp, "i", guards_ok))
+    assert not bad, bad[:20]
