@@ -63,7 +63,8 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
     for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
-        const int strip = u % D.n_strips, seg = D.seg_base + u / D.n_strips;
+        const int q = u / D.n_strips;
+        const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
         if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr))
             break;
     }

@@ -39,6 +39,7 @@ struct LevelDesc {
     int w, h;
     int n_strips, seg_pairs, n_segs;
     int seg_base;  // first segment of this launch (a launch may cover a sub-range)
+    int reverse;   // hand out the segments bottom-up (the previous level ended there)
     int rows_only;
     int tmap;      // inverse: the tensor maps of the launch are valid (set by launch_level)
     const float *in[4];
