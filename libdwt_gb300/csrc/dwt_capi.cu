@@ -307,6 +307,7 @@ static cudaError_t dense_forward_levels(const float *in, long long in_pitch, flo
     scratch_frames(W, H, J, scratch, buf, p);
     const int j0 = std::max(coarse_level(W, H, J), j_begin);
     for (int j = j_begin; j < j0; ++j) {
+        const NvtxRange range("level %d forward %dx%d", j, ceil_div_pow2(W, j), ceil_div_pow2(H, j));
         LevelDesc d = fwd_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
         plan_level(d, seg_hint, false);
         d.reverse = kAlternateOrder && ((j - j_begin) & 1);
@@ -341,6 +342,7 @@ static cudaError_t dense_inverse_levels(const float *in, long long in_pitch, flo
         jtop = j0;
     }
     for (int j = jtop; j >= j_end; --j) {
+        const NvtxRange range("level %d inverse %dx%d", j - 1, ceil_div_pow2(W, j - 1), ceil_div_pow2(H, j - 1));
         LevelDesc d = inv_desc(in, in_pitch, out, out_pitch, W, H, J, j, buf, p);
         plan_level(d, seg_hint, true);
         d.reverse = kAlternateOrder && ((jtop - j) & 1);
@@ -763,6 +765,8 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
         return set_error(DWT_GPU_EINVAL);
     }
 
+    const NvtxRange range("dwt 2D %s %s %dx%d j=%d", wavelet == CDF97 ? "cdf97" : "cdf53",
+                          inverse ? "inverse" : "forward", ix, iy, J);
     LaneGuard lane_guard(ctx());
     Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
@@ -1011,6 +1015,8 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
         log_error("stride %d smaller than a sample\n", stride);
         return set_error(DWT_GPU_EINVAL);
     }
+    const NvtxRange range("dwt 1D %s %s N=%d", wavelet == CDF97 ? "cdf97" : "cdf53", inverse ? "inverse" : "forward",
+                          N);
     LaneGuard lane_guard(ctx());
     Lane &c = lane_guard.get();
     cudaStream_t s = c.stream;
@@ -1239,6 +1245,8 @@ int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_
                                  cudaMemcpyDeviceToDevice, s));
         return 0;
     }
+    const NvtxRange range("dwt 2D device %s %s %dx%d j=%d", wavelet == CDF97 ? "cdf97" : "cdf53",
+                          inverse ? "inverse" : "forward", w, h, J);
     Context &c = ctx();
     long long p0, p1;
     const size_t sf = dense_scratch_floats(w, h, J, &p0, &p1);

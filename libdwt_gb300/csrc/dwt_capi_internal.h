@@ -2,7 +2,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
+#include <cstdio>
 #include <mutex>
 #include <vector>
 
@@ -51,6 +53,23 @@ struct Context {
 
 Context &ctx();
 void ctx_finish();
+
+// A named range on the calling thread for the duration of a scope, shown
+// by Nsight Systems on the timeline (free when no tool is attached).
+class NvtxRange {
+public:
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    template <typename... A>
+    NvtxRange(const char *fmt, A... args)
+    {
+        char buf[96];
+        snprintf(buf, sizeof buf, fmt, args...);
+        nvtxRangePushA(buf);
+    }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Holds a drop-in lane for the duration of a call: a free one if any, else
 // the calling thread's own (waiting for it).
