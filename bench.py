@@ -356,32 +356,51 @@ def main():
         raise SystemExit("device error during the timed region")
     px_step = 2 * W * H
     value = replica_value(ws, args.steps, px_step, ms)
+    # algorithmic bytes of one step: 8 B per pixel of every level, both
+    # directions
+    step_bytes = 2 * sum(8 * (-(-W // (1 << k))) * (-(-H // (1 << k))) for k in range(J))
 
     # parity spot check of the benchmarked output (outside the timed region):
     # the reconstruction is within the reference's round-trip tolerance
     err_rt = float((rec - src).abs().max().item())
 
-    # dominant kernel alone: forward level 0 (16384^2 -> four bands)
+    # level 0 alone, both directions (16384^2 <-> four bands), each timed
+    # with CUDA events over `reps` back-to-back launches; the slower one is
+    # the dominant kernel of the step (its template instance runs every level
+    # of its direction and has the larger share of the step's device time)
     bands = torch.empty_like(src)
     ll = torch.empty((H // 2, W // 2), dtype=torch.float32, device="cuda")
+    rec0 = torch.empty_like(src)
     hw, hh = W // 2, H // 2
     outs = [ll.data_ptr(), bands.data_ptr() + hw * 4, bands.data_ptr() + hh * W * 4,
             bands.data_ptr() + (hh * W + hw) * 4]
     pitches = [hw * 4, W * 4, W * 4, W * 4]
     reps = max(1, args.level_reps)
-    for _ in range(3):
-        D.level_dev("cdf97", False, W, H, [src.data_ptr()], [W * 4], outs, pitches, sptr)
-    torch.cuda.synchronize()
-    k0 = torch.cuda.Event(enable_timing=True)
-    k1 = torch.cuda.Event(enable_timing=True)
+
+    def level0(inverse):
+        if inverse:
+            D.level_dev("cdf97", True, W, H, outs, pitches, [rec0.data_ptr()], [W * 4], sptr)
+        else:
+            D.level_dev("cdf97", False, W, H, [src.data_ptr()], [W * 4], outs, pitches, sptr)
+
+    level_ms = {}
     tk0 = time.time()
-    k0.record(stream)
-    for _ in range(reps):
-        D.level_dev("cdf97", False, W, H, [src.data_ptr()], [W * 4], outs, pitches, sptr)
-    k1.record(stream)
-    torch.cuda.synchronize()
+    for inverse in (False, True):
+        for _ in range(3):
+            level0(inverse)
+        torch.cuda.synchronize()
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(reps):
+            level0(inverse)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        level_ms[inverse] = k0.elapsed_time(k1) / reps
     tk1 = time.time()
-    kms = k0.elapsed_time(k1) / reps
+    level0_rt_err = float((rec0 - src).abs().max().item())  # one level forward, then inverse
+    dom_inv = level_ms[True] >= level_ms[False]
+    kms = level_ms[dom_inv]
     alg_bytes = 8 * W * H
     achieved = alg_bytes / (kms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
@@ -389,7 +408,8 @@ def main():
     tfile = os.path.join(ROOT, "profiles", "level0_traffic.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            tj = json.load(f)
+        traffic = tj.get("inverse" if dom_inv else "forward", {}).get("dram_bytes_per_launch")
 
     # e2e through the drop-in C ABI on a pinned host image
     if args.skip_e2e:
@@ -430,11 +450,21 @@ def main():
                     "h2d_bytes_per_step": 2 * W * H * 4, "d2h_bytes_per_step": 2 * W * H * 4,
                     "api": "dwt_cdf97_2f_s + dwt_cdf97_2i_s on pinned host memory",
                     "roundtrip_max_abs_err": err_e2e},
-            "roofline": {"bound": "hbm", "kernel": "level_kernel<4,false> (CDF 9/7 forward, level 0)",
+            "roofline": {"bound": "hbm",
+                         "kernel": ("level_kernel<4,true> (CDF 9/7 inverse, level 0)" if dom_inv
+                                    else "level_kernel<4,false> (CDF 9/7 forward, level 0)"),
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-                         "launch_ms": round(kms, 4)},
+                         "launch_ms": round(kms, 4),
+                         "other_level0": {
+                             "kernel": ("level_kernel<4,false> (CDF 9/7 forward, level 0)" if dom_inv
+                                        else "level_kernel<4,true> (CDF 9/7 inverse, level 0)"),
+                             "launch_ms": round(level_ms[not dom_inv], 4),
+                             "frac": round(alg_bytes / (level_ms[not dom_inv] / 1e3) / 1e9 / peak, 4)},
+                         "level0_roundtrip_max_abs_err": level0_rt_err,
+                         "step_bytes": step_bytes,
+                         "step_frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4)},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": args.steps * 2 * D.lib().dwt_gpu_dense_launches(W, H, J),
@@ -582,6 +612,13 @@ def run_serve_extra(D, torch, seconds: float):
     reqs = [D.Server.request(src, None, "cdf97" if wav[k] == 0 else "cdf53", bool(inv[k]), int(j[k]), tag=k,
                              w=int(w[k]), h=int(h[k])) for k in range(len(t))]
     srv = D.Server(budget_bytes=64 << 30, n_streams=8)
+    # set-up outside the measured replay: the arena's device memory and one
+    # request of every path, so no allocation or kernel loading happens
+    # while requests are served
+    t0 = time.perf_counter()
+    srv.reserve(16 << 30)
+    reserve_s = time.perf_counter() - t0
+    st0 = srv.stats()
     t0 = time.perf_counter()
     lat = srv.replay(t, reqs, timeout_s=600)
     wall = time.perf_counter() - t0
@@ -591,7 +628,10 @@ def run_serve_extra(D, torch, seconds: float):
            "c3_sustained_mpx_s": round(px / wall / 1e6, 1), "c3_p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
            "c3_p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
            "c3_max_ms": round(float(lat.max()) * 1e3, 3), "c3_launches": st["launches"],
-           "c3_peak_bytes": st["peak_bytes"], "c3_budget_bytes": st["budget_bytes"]}
+           "c3_peak_bytes": st["peak_bytes"], "c3_budget_bytes": st["budget_bytes"],
+           "c3_reserve_s": round(reserve_s, 3), "c3_arena_bytes": st["arena_bytes"],
+           "c3_device_allocs_in_replay": st["device_allocs"] - st0["device_allocs"],
+           "c3_max_dispatch_ms": round(st["max_dispatch_ns"] / 1e6, 3)}
     # capacity: the first 2 s of the same trace offered 5x faster (100k req/s)
     k2 = int(np.searchsorted(t, 2.0))
     t0 = time.perf_counter()

@@ -419,7 +419,9 @@ DWT_EXPORT int dwt_gpu_1_d(int wavelet, int inverse, const double *a, const doub
  * 16-byte aligned).  The result is the reference's in-place layout written to
  * dst.  j_levels < 0 means the full depth; the achieved depth is returned
  * (>= 0) or an error code (< 0).  stream is a cudaStream_t (0 = default).
- * Work is enqueued; the call does not synchronize. */
+ * Out of place only: frames whose byte spans intersect return DWT_GPU_EINVAL
+ * (unless j_levels resolves to 0).  Work is enqueued; the call does not
+ * synchronize; dwt_gpu_sync_check reports a device-side error of it. */
 DWT_EXPORT int dwt_gpu_2_dev(int wavelet, int inverse, const float *src, long long src_pitch_bytes,
                   float *dst, long long dst_pitch_bytes, int w, int h, int j_levels,
                   int decompose_one, void *stream);
@@ -446,7 +448,11 @@ DWT_EXPORT int dwt_gpu_dense_launches(int w, int h, int j_levels);
  * code), and the context stays usable.  DWT_GPU_EINVAL for iterations <= 0. */
 DWT_EXPORT int dwt_gpu_selftest_wait_timeout(int iterations);
 
-/* Waits for all device work and reports (and clears) a device-side error. */
+/* Waits for all device work and reports (and clears) a device-side error:
+ * DWT_GPU_EDEVICE when a bounded device-side wait of the library's own
+ * context or of dwt_gpu_2_dev_noalloc (on any device it ran on) gave up.
+ * Creates nothing: a process that only ever called dwt_gpu_2_dev_noalloc
+ * can check its work without the pooled context being set up. */
 DWT_EXPORT int dwt_gpu_sync_check(void);
 
 /* No counterpart in the reference.  dwt_gpu_2_dev without any device
@@ -455,13 +461,26 @@ DWT_EXPORT int dwt_gpu_sync_check(void);
  * byte, and latency-critical loops that cannot risk cudaMalloc/cudaFree (which
  * may synchronize the device).  Its inter-level scratch is a fixed ~5.2 MB
  * array inside the library (held by every GPU that loads it, until exit);
- * images up to 2048 x 2048 fit, larger ones return DWT_GPU_EINVAL.  The first
- * call on a device looks the array up (make it before any stream capture).
- * All calls share the array: calls whose GPU work overlaps race. */
+ * images up to 2048 x 2048 fit, larger ones return DWT_GPU_EINVAL, and so do
+ * overlapping source and destination frames (out of place only).  The first
+ * call on a device looks the array up (make it before any stream capture); a
+ * cudaDeviceReset invalidates that address, so make no further call after
+ * one.  All calls share the array: calls whose GPU work overlaps race.  The
+ * call enqueues and returns; dwt_gpu_sync_check reports a device-side wait
+ * that gave up (DWT_GPU_EDEVICE). */
 DWT_EXPORT int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
                                      long long src_pitch_bytes, float *dst,
                                      long long dst_pitch_bytes, int w, int h, int j_levels,
                                      int decompose_one, void *stream);
+
+/* No counterpart in the reference.  Test hook of the error path above: a
+ * one-warp kernel on the default stream waits (bounded, `iterations` tries)
+ * on an mbarrier that nothing completes and sets the error word of
+ * dwt_gpu_2_dev_noalloc on the current device, as a level kernel does when its
+ * staged data never arrives; no fault, no allocation.  Enqueues and returns;
+ * dwt_gpu_sync_check then reports DWT_GPU_EDEVICE.  DWT_GPU_EINVAL for
+ * iterations <= 0. */
+DWT_EXPORT int dwt_gpu_selftest_noalloc_wait_timeout(int iterations);
 
 /* Batched strided 1D level, in place, device or host memory: `count`
  * signals of N samples, signal s at base + (s / group) * group_stride +
@@ -545,6 +564,9 @@ typedef struct {
 typedef struct {
     long long submitted, completed, launches, pending;
     long long bytes_in_use, peak_bytes, budget_bytes;
+    long long arena_bytes;     /* device memory the server's arena holds */
+    long long device_allocs;   /* cudaMalloc / cudaHostAlloc calls of the server since it started */
+    long long max_dispatch_ns; /* longest dispatcher iteration since the last reserve / replay */
 } dwt_gpu_server_stats_t;
 
 typedef struct dwt_gpu_server dwt_gpu_server;
@@ -555,6 +577,15 @@ typedef struct dwt_gpu_server dwt_gpu_server;
  * overlap on the device.  params = NULL uses (32, 32, 4). */
 DWT_EXPORT int dwt_gpu_server_create(dwt_gpu_server **out, long long budget_bytes, int n_streams,
                                      const dwt_gpu_batch_params *params);
+/* Reserves `bytes` (at most the budget) of device memory for the server's
+ * arena, out of which every request's output and scratch are carved, and runs
+ * one small and one large request of each wavelet and direction so that every
+ * kernel is loaded and configured.  Call it once after create, before the
+ * first client request: afterwards no cudaMalloc / cudaFree runs while
+ * requests are served unless a request fits nowhere in the reserved slabs
+ * (the arena then grows by one slab, up to the budget).  Without it the
+ * arena grows on demand, 1 GiB at a time. */
+DWT_EXPORT int dwt_gpu_server_reserve(dwt_gpu_server *s, long long bytes);
 /* Queues a request (never blocks); DWT_GPU_EBUSY if it alone exceeds the budget. */
 DWT_EXPORT int dwt_gpu_server_submit(dwt_gpu_server *s, const dwt_gpu_request *r, long long *id);
 /* Takes up to `max` completions. */

@@ -56,7 +56,8 @@ class Completion(C.Structure):
 class ServerStats(C.Structure):
     """dwt_gpu_server_stats_t (include/libdwt.h)."""
     _fields_ = [("submitted", _ll), ("completed", _ll), ("launches", _ll), ("pending", _ll),
-                ("bytes_in_use", _ll), ("peak_bytes", _ll), ("budget_bytes", _ll)]
+                ("bytes_in_use", _ll), ("peak_bytes", _ll), ("budget_bytes", _ll), ("arena_bytes", _ll),
+                ("device_allocs", _ll), ("max_dispatch_ns", _ll)]
 
 
 class BatchParams(C.Structure):
@@ -103,6 +104,7 @@ def lib():
         L.dwt_gpu_batch_destroy.argtypes = [C.c_void_p]
         L.dwt_gpu_sync_check.restype = _i
         L.dwt_gpu_server_create.argtypes = [C.POINTER(C.c_void_p), _ll, _i, C.POINTER(BatchParams)]
+        L.dwt_gpu_server_reserve.argtypes = [C.c_void_p, _ll]
         L.dwt_gpu_server_submit.argtypes = [C.c_void_p, C.POINTER(Request), C.POINTER(_ll)]
         L.dwt_gpu_server_poll.argtypes = [C.c_void_p, C.POINTER(Completion), _i, C.POINTER(_i)]
         L.dwt_gpu_server_drain.argtypes = [C.c_void_p, C.c_double]
@@ -377,6 +379,10 @@ class Server:
                        src.stride(0) * 4 if hasattr(src, "stride") else 0,
                        None if dst is None else dst.data_ptr(), 0 if dst is None else dst.stride(0) * 4,
                        ww, hh, j_levels, 0, _WAVELETS[wavelet], 1 if inverse else 0, tag)
+
+    def reserve(self, nbytes: int) -> None:
+        """Reserve the arena and load every kernel (dwt_gpu_server_reserve)."""
+        _check(lib().dwt_gpu_server_reserve(self._h, nbytes))
 
     def submit(self, req: Request) -> int:
         i = _ll()

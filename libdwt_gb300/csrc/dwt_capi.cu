@@ -1245,6 +1245,10 @@ int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_
                                  cudaMemcpyDeviceToDevice, s));
         return 0;
     }
+    if (frames_overlap(src, src_pitch_bytes, dst, dst_pitch_bytes, w, h)) {
+        log_error("dwt_gpu_2_dev: the source and destination frames overlap (out of place only)\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
     const NvtxRange range("dwt 2D device %s %s %dx%d j=%d", wavelet == CDF97 ? "cdf97" : "cdf53",
                           inverse ? "inverse" : "forward", w, h, J);
     Context &c = ctx();
@@ -1278,6 +1282,12 @@ __global__ void wait_timeout_kernel(uint32_t iterations, int *err)
     __syncwarp();
     const bool done = mbar_wait_bounded(&bar, 0, iterations);  // no arrival is ever made
     if (!__all_sync(0xffffffffu, done) && threadIdx.x == 0) atomicCAS(err, 0, int(kErrWaitTimeout));
+}
+
+cudaError_t launch_wait_timeout(uint32_t iterations, int *err, cudaStream_t s)
+{
+    wait_timeout_kernel<<<1, 32, 0, s>>>(iterations, err);
+    return cudaGetLastError();
 }
 
 }  // namespace dwt
@@ -1435,9 +1445,19 @@ int dwt_gpu_selftest_wait_timeout(int iterations)
 
 int dwt_gpu_sync_check(void)
 {
-    Context &c = ctx();
+    // the pooled context is only checked when it exists: a caller of the
+    // allocation-free entry point must be able to check its work without
+    // having the context (and its allocations) created
+    Context *c = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_init_mu);
+        c = g_ctx;
+        if (c) cudaSetDevice(c->device);
+    }
     if (cudaDeviceSynchronize() != cudaSuccess) return set_error(DWT_GPU_ECUDA);
-    return set_error(check_device_error(c));
+    const int rc_noalloc = noalloc_device_error();
+    const int rc_ctx = c ? check_device_error(*c) : DWT_GPU_OK;
+    return set_error(rc_ctx != DWT_GPU_OK ? rc_ctx : rc_noalloc);
 }
 
 void dwt_cdf97_2f_s(void *ptr, int stride_x, int stride_y, int ox, int oy, int ix, int iy, int *j_max_ptr,

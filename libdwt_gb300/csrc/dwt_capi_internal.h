@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -88,6 +89,27 @@ void log_error(const char *fmt, ...);
 int set_error(int code);
 MemKind classify(const void *p);
 int ceil_log2_int(int x);
+
+// Whether the byte spans of two w x h float frames (first sample to last
+// sample of the last row) intersect.  The out-of-place device forms refuse
+// such pairs: a level kernel would read samples another tile already wrote.
+inline bool frames_overlap(const void *a, long long a_pitch_bytes, const void *b, long long b_pitch_bytes, int w,
+                           int h)
+{
+    const unsigned long long a0 = reinterpret_cast<uintptr_t>(a), b0 = reinterpret_cast<uintptr_t>(b);
+    const unsigned long long a1 = a0 + (unsigned long long)(h - 1) * a_pitch_bytes + 4ull * w;
+    const unsigned long long b1 = b0 + (unsigned long long)(h - 1) * b_pitch_bytes + 4ull * w;
+    return a0 < b1 && b0 < a1;
+}
+
+// Reads and clears the error word of the allocation-free entry point on every
+// device it ran on (DWT_GPU_OK when it never ran, DWT_GPU_EDEVICE when a
+// device-side wait of it gave up); the caller has synchronised the devices.
+int noalloc_device_error();
+
+// Enqueues a one-warp kernel whose bounded mbarrier wait is never satisfied:
+// it gives up after `iterations` tries and sets *err (no fault).
+cudaError_t launch_wait_timeout(uint32_t iterations, int *err, cudaStream_t s);
 
 // Scratch floats the dense pipelines need for a W x H image over J levels.
 size_t dense_scratch_floats(int W, int H, int J, long long *pitch0, long long *pitch1);

@@ -29,6 +29,14 @@
 // on the GPU -- on different streams, or from different host threads without
 // ordering between their streams -- race on the array and corrupt each
 // other's results.
+//
+// Errors: arguments are checked before anything is enqueued (overlapping
+// source and destination frames included: the level kernels work out of
+// place).  A bounded device-side wait that gives up sets the error word;
+// dwt_gpu_sync_check reads and clears it (for every device this entry point
+// ran on) without creating the library's pooled context.  The device
+// addresses are cached per device for the life of the process: a
+// cudaDeviceReset invalidates them, and no call may follow one.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -77,6 +85,32 @@ cudaError_t noalloc_addresses(float **scratch, int **err)
 
 }  // namespace
 
+int noalloc_device_error()
+{
+    // every device this entry point has run on: its word is read and cleared
+    // with that device current (the caller synchronised the devices)
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return DWT_GPU_ECUDA;
+    int rc = DWT_GPU_OK;
+    std::lock_guard<std::mutex> g(g_setup_mu);
+    for (int dev = 0; dev < kMaxDevices; ++dev) {
+        if (!g_err_addr[dev]) continue;
+        int h = 0;
+        if (cudaSetDevice(dev) != cudaSuccess ||
+            cudaMemcpy(&h, g_err_addr[dev], sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = DWT_GPU_ECUDA;
+            continue;
+        }
+        if (h) {
+            cudaMemset(g_err_addr[dev], 0, sizeof(int));
+            log_error("dwt_gpu_2_dev_noalloc: device-side wait gave up on device %d (code %d)\n", dev, h);
+            if (rc == DWT_GPU_OK) rc = DWT_GPU_EDEVICE;
+        }
+    }
+    cudaSetDevice(cur);
+    return rc;
+}
+
 }  // namespace dwt
 
 using namespace dwt;
@@ -85,6 +119,7 @@ extern "C" int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
                                      float *dst, long long dst_pitch_bytes, int w, int h, int j_levels,
                                      int decompose_one, void *stream)
 {
+    set_error(DWT_GPU_OK);
     if ((wavelet != CDF97 && wavelet != CDF53) || w <= 0 || h <= 0 || !src || !dst ||
         (src_pitch_bytes % 16) != 0 || (reinterpret_cast<uintptr_t>(src) & 15) != 0 ||
         (dst_pitch_bytes % 4) != 0 || src_pitch_bytes < 4LL * w || dst_pitch_bytes < 4LL * w) {
@@ -109,6 +144,10 @@ extern "C" int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
             return set_error(DWT_GPU_ECUDA);
         return 0;
     }
+    if (frames_overlap(src, src_pitch_bytes, dst, dst_pitch_bytes, w, h)) {
+        log_error("dwt_gpu_2_dev_noalloc: the source and destination frames overlap (out of place only)\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
     float *scratch = nullptr;
     int *err = nullptr;
     cudaError_t e = noalloc_addresses(&scratch, &err);
@@ -124,4 +163,19 @@ extern "C" int dwt_gpu_2_dev_noalloc(int wavelet, int inverse, const float *src,
     }
     set_error(DWT_GPU_OK);
     return J;
+}
+
+extern "C" int dwt_gpu_selftest_noalloc_wait_timeout(int iterations)
+{
+    set_error(DWT_GPU_OK);
+    if (iterations <= 0) return set_error(DWT_GPU_EINVAL);
+    float *scratch = nullptr;
+    int *err = nullptr;
+    cudaError_t e = noalloc_addresses(&scratch, &err);
+    if (e == cudaSuccess) e = launch_wait_timeout(uint32_t(iterations), err, nullptr);
+    if (e != cudaSuccess) {
+        log_error("dwt_gpu_selftest_noalloc_wait_timeout: CUDA error %s\n", cudaGetErrorString(e));
+        return set_error(DWT_GPU_ECUDA);
+    }
+    return DWT_GPU_OK;
 }

@@ -13,8 +13,15 @@
 //     a mixed stream) run the per-level pipeline of the plain drop-in, which
 //     is at its best on large images;
 //   - polls the micro-batches' completion events, returns their buffers to
-//     the pool (they stay cached there, not freed) and stamps each request's
-//     completion time.
+//     the server's arena and stamps each request's completion time.
+// Device memory: every request's output (when the client gave none) and
+// inter-level scratch come from the server's own arena (dwt_arena.h), slabs
+// reserved at set-up by dwt_gpu_server_reserve, so that no cudaMalloc or
+// cudaFree runs on the dispatcher while requests are served; each flight
+// keeps its descriptor buffers (device and pinned host) for its lifetime.
+// dwt_gpu_server_reserve also runs one small and one large request of every
+// wavelet and direction, so the kernels are loaded and configured before the
+// first client request.
 // Latency is arrival (submit) to completion as seen by the dispatcher.
 // dwt_gpu_server_replay drives a recorded arrival trace in real time (the
 // benchmark's Poisson stream) from the calling thread.
@@ -31,6 +38,7 @@
 #include <vector>
 
 #include "../../include/libdwt.h"
+#include "dwt_arena.h"
 #include "dwt_batch.cuh"
 #include "dwt_capi_internal.h"
 
@@ -58,12 +66,17 @@ struct Flight {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     std::vector<Req> reqs;
-    void *d_desc = nullptr;  // images + items + counters, one pooled block
-    size_t desc_bytes = 0;
-    void *h_desc = nullptr;  // pinned staging of the descriptors
+    void *d_desc = nullptr;  // images + items + counters (kept, grown when too small)
+    size_t d_cap = 0;
+    void *h_desc = nullptr;  // pinned staging of the descriptors (kept, grown likewise)
     size_t h_cap = 0;
     bool busy = false;
 };
+
+// Descriptor capacity each flight starts with (device and pinned host): a
+// micro-batch of small requests holds at most about kFlightPixels / 4096 work
+// items, far below this.
+constexpr size_t kDescBytes = size_t(8) << 20;
 
 }  // namespace
 
@@ -83,6 +96,9 @@ struct dwt_gpu_server {
     std::atomic<bool> stop{false};
     std::thread dispatcher;
     int device = 0;
+    dwt::Arena arena;
+    std::atomic<long long> desc_allocs{0};     // descriptor buffers grown after set-up
+    std::atomic<long long> max_loop_ns{0};     // longest dispatcher iteration
 };
 
 namespace {
@@ -142,12 +158,33 @@ void launch_flight(dwt_gpu_server *S, Flight &f)
     const size_t off_items = (img_b + 255) & ~size_t(255);
     const size_t off_cnt = (off_items + item_b + 255) & ~size_t(255);
     const size_t total = off_cnt + cnt_b;
-    f.d_desc = c.pool.alloc(total, f.stream);
-    f.desc_bytes = total;
+    if (f.d_cap < total) {
+        // only a micro-batch beyond kDescBytes gets here; the flight's stream
+        // is idle (the flight was free), so the old buffers can go at once
+        S->desc_allocs++;
+        if (f.d_desc) cudaFree(f.d_desc);
+        f.d_cap = std::max(total, 2 * f.d_cap);
+        if (cudaMalloc(&f.d_desc, f.d_cap) != cudaSuccess) {
+            cudaGetLastError();
+            f.d_desc = nullptr;
+            f.d_cap = 0;
+        }
+    }
     if (f.h_cap < off_cnt) {
+        S->desc_allocs++;
         if (f.h_desc) cudaFreeHost(f.h_desc);
-        f.h_cap = std::max(off_cnt, f.h_cap * 2);
-        cudaHostAlloc(&f.h_desc, f.h_cap, cudaHostAllocDefault);
+        f.h_cap = std::max(off_cnt, 2 * f.h_cap);
+        if (cudaHostAlloc(&f.h_desc, f.h_cap, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            f.h_desc = nullptr;
+            f.h_cap = 0;
+        }
+    }
+    if (!f.d_desc || !f.h_desc) {
+        for (Req &q : f.reqs) q.status = DWT_GPU_ENOMEM;
+        cudaEventRecord(f.done, f.stream);
+        f.busy = true;
+        return;
     }
     char *h = static_cast<char *>(f.h_desc);
     memcpy(h, imgs.data(), img_b);
@@ -190,23 +227,21 @@ void launch_flight(dwt_gpu_server *S, Flight &f)
 void dispatcher_loop(dwt_gpu_server *S)
 {
     cudaSetDevice(S->device);
-    dwt::Context &c = dwt::ctx();
     std::vector<Req> admitted;
     while (!S->stop.load()) {
         bool did = false;
+        const double t_loop = now_s();
         // 1. completions
         for (Flight &f : S->flights) {
             if (!f.busy || cudaEventQuery(f.done) != cudaSuccess) continue;
             const double t = now_s();
             std::vector<dwt_gpu_completion> done;
             for (Req &q : f.reqs) {
-                if (q.pooled) c.pool.release(q.pooled, f.stream);
-                if (q.scratch) c.pool.release(q.scratch, f.stream);
+                S->arena.free(q.pooled);
+                S->arena.free(q.scratch);
                 S->used -= q.bytes;
                 done.push_back({q.id, q.r.tag, q.status, q.t_submit, q.t_admit, t});
             }
-            c.pool.release(f.d_desc, f.stream);
-            f.d_desc = nullptr;
             f.reqs.clear();
             f.busy = false;
             {
@@ -235,6 +270,22 @@ void dispatcher_loop(dwt_gpu_server *S)
                 const int J = levels_of(q.r);
                 const size_t need = request_bytes(q.r, J);
                 if (S->used + need > S->budget) break;
+                long long p0, p1;
+                const size_t sf = dwt::dense_scratch_floats(q.r.w, q.r.h, J, &p0, &p1);
+                void *scratch = sf ? S->arena.alloc(sf * 4 + 256) : nullptr;
+                void *pooled = q.r.dst ? nullptr : S->arena.alloc(size_t(q.r.w) * q.r.h * 4 + 256);
+                if ((sf && !scratch) || (!q.r.dst && !pooled)) {
+                    S->arena.free(scratch);
+                    S->arena.free(pooled);
+                    // the arena is full (or fragmented) at its cap: wait for
+                    // completions to free memory; with nothing in flight its
+                    // slabs are too small for this request, so they are
+                    // replaced by one that holds it (a rare, synchronising path)
+                    if (S->used.load() == 0 && S->arena.release_if_idle()) continue;
+                    break;
+                }
+                q.scratch = scratch;
+                q.pooled = static_cast<float *>(pooled);
                 flight_px += (long long)q.r.w * q.r.h;
                 q.bytes = need;
                 S->used += need;
@@ -245,14 +296,7 @@ void dispatcher_loop(dwt_gpu_server *S)
             g.unlock();
             if (!admitted.empty()) {
                 const double t = now_s();
-                for (Req &q : admitted) {
-                    q.t_admit = t;
-                    const int J = levels_of(q.r);
-                    long long p0, p1;
-                    const size_t sf = dwt::dense_scratch_floats(q.r.w, q.r.h, J, &p0, &p1);
-                    q.scratch = sf ? c.pool.alloc(sf * 4 + 256, free_f->stream) : nullptr;
-                    if (!q.r.dst) q.pooled = static_cast<float *>(c.pool.alloc(size_t(q.r.w) * q.r.h * 4 + 256, free_f->stream));
-                }
+                for (Req &q : admitted) q.t_admit = t;
                 free_f->reqs.swap(admitted);
                 admitted.clear();
                 S->admitted += (long long)free_f->reqs.size();
@@ -261,6 +305,9 @@ void dispatcher_loop(dwt_gpu_server *S)
                 did = true;
             }
         }
+        const double t_end = now_s();
+        const long long ns = (long long)((t_end - t_loop) * 1e9);
+        if (ns > S->max_loop_ns.load()) S->max_loop_ns = ns;
         if (!did) std::this_thread::sleep_for(std::chrono::microseconds(5));
     }
 }
@@ -280,10 +327,16 @@ int dwt_gpu_server_create(dwt_gpu_server **out, long long budget_bytes, int n_st
     S->params = params ? *params : dwt_gpu_batch_params{32, 32, 4};
     if (S->params.seg_pairs <= 0) S->params.seg_pairs = 32;
     if (S->params.ctas_per_sm <= 0) S->params.ctas_per_sm = 4;
+    S->arena.set_cap(S->budget);
     S->flights.resize(std::max(1, n_streams));
     for (Flight &f : S->flights) {
         cudaStreamCreateWithFlags(&f.stream, cudaStreamNonBlocking);
         cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
+        if (cudaMalloc(&f.d_desc, kDescBytes) == cudaSuccess) f.d_cap = kDescBytes;
+        else f.d_desc = nullptr;
+        if (cudaHostAlloc(&f.h_desc, kDescBytes, cudaHostAllocDefault) == cudaSuccess) f.h_cap = kDescBytes;
+        else f.h_desc = nullptr;
+        cudaGetLastError();
     }
     S->dispatcher = std::thread(dispatcher_loop, S);
     *out = S;
@@ -342,7 +395,67 @@ int dwt_gpu_server_stats(dwt_gpu_server *S, dwt_gpu_server_stats_t *st)
     st->bytes_in_use = (long long)S->used.load();
     st->peak_bytes = (long long)S->peak;
     st->budget_bytes = (long long)S->budget;
+    const dwt::Arena::Stats a = S->arena.stats();
+    st->arena_bytes = (long long)a.reserved;
+    st->device_allocs = a.device_allocs + S->desc_allocs.load();
+    st->max_dispatch_ns = S->max_loop_ns.load();
     return DWT_GPU_OK;
+}
+
+int dwt_gpu_server_reserve(dwt_gpu_server *S, long long bytes)
+{
+    if (!S || bytes < 0) return dwt::set_error(DWT_GPU_EINVAL);
+    if (!S->arena.reserve(size_t(bytes))) return dwt::set_error(DWT_GPU_ENOMEM);
+    // warm-up: one request of each path (batched kernel, small and odd; the
+    // per-level pipeline with the coarse kernel) per wavelet and direction,
+    // out of a zeroed source, so that every kernel the server launches is
+    // loaded and configured now; their completions are dropped
+    const int kw = 2048, kh = 1024;
+    float *src = nullptr;
+    if (cudaMalloc(&src, size_t(kw) * kh * 4) != cudaSuccess) {
+        cudaGetLastError();
+        return dwt::set_error(DWT_GPU_ENOMEM);
+    }
+    cudaMemset(src, 0, size_t(kw) * kh * 4);
+    cudaDeviceSynchronize();
+    std::vector<long long> ids;
+    const int sizes[3][2] = {{64, 64}, {333, 97}, {kw, kh}};
+    for (int wav : {DWT_GPU_CDF97, DWT_GPU_CDF53})
+        for (int inv = 0; inv < 2; ++inv)
+            for (const auto &sz : sizes) {
+                dwt_gpu_request r{};
+                r.src = src;
+                r.src_pitch_bytes = (long long)kw * 4;
+                r.dst = nullptr;
+                r.w = sz[0];
+                r.h = sz[1];
+                r.j_levels = 6;
+                r.wavelet = wav;
+                r.inverse = inv;
+                long long id = 0;
+                if (dwt_gpu_server_submit(S, &r, &id) == DWT_GPU_OK) ids.push_back(id);
+            }
+    const int rc = dwt_gpu_server_drain(S, 120.0);
+    cudaFree(src);
+    {
+        // the warm-up requests are not the clients': drop their completions
+        // and start the counters afresh
+        std::lock_guard<std::mutex> g(S->mu);
+        S->completed.erase(std::remove_if(S->completed.begin(), S->completed.end(),
+                                          [&](const dwt_gpu_completion &c) {
+                                              return std::find(ids.begin(), ids.end(), c.id) != ids.end();
+                                          }),
+                           S->completed.end());
+        if (rc == DWT_GPU_OK) {
+            S->submitted -= (long long)ids.size();
+            S->finished -= (long long)ids.size();
+            S->admitted -= (long long)ids.size();
+            S->launches = 0;
+            S->peak = S->used.load();
+        }
+    }
+    S->max_loop_ns = 0;
+    return dwt::set_error(rc);
 }
 
 int dwt_gpu_server_replay(dwt_gpu_server *S, int n, const double *arrival_s, const dwt_gpu_request *reqs,
@@ -350,6 +463,7 @@ int dwt_gpu_server_replay(dwt_gpu_server *S, int n, const double *arrival_s, con
 {
     if (!S || n < 0 || (n > 0 && (!arrival_s || !reqs || !latency_s))) return dwt::set_error(DWT_GPU_EINVAL);
     std::vector<long long> ids(n, 0);
+    S->max_loop_ns = 0;
     const double t0 = now_s();
     for (int i = 0; i < n; ++i) {
         const double due = t0 + arrival_s[i];
@@ -380,10 +494,9 @@ void dwt_gpu_server_destroy(dwt_gpu_server *S)
     dwt_gpu_server_drain(S, 60.0);
     S->stop = true;
     if (S->dispatcher.joinable()) S->dispatcher.join();
-    dwt::Context &c = dwt::ctx();
     for (Flight &f : S->flights) {
         cudaStreamSynchronize(f.stream);
-        if (f.d_desc) c.pool.release(f.d_desc, f.stream);
+        if (f.d_desc) cudaFree(f.d_desc);
         if (f.h_desc) cudaFreeHost(f.h_desc);
         cudaEventDestroy(f.done);
         cudaStreamDestroy(f.stream);

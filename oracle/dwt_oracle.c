@@ -8,8 +8,8 @@
  *
  * Parity is pinned two ways (see tests/test_oracle_pin.py):
  *   - bit-exact against golden vectors produced by the reference itself
- *     (tests/golden/make_golden.py runs src/libdwt.c compiled by
- *     oracle/build_ref.sh), and
+ *     (tests/golden/make_golden.py runs src/libdwt.c compiled by the `ref`
+ *     target of oracle/Makefile), and
  *   - bit-exact against the compiled reference directly where it is present.
  *
  * Arithmetic rules that make the float path bit-identical to the reference:
@@ -33,6 +33,7 @@
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+#include <stdint.h>
 
 /* Lifting constants, src/libdwt.c:541-573. */
 static const float  cdf97_p1_s =  1.58613434342059;
@@ -510,6 +511,37 @@ void oracle_cdf97_1_batch_s(void *base, int N, int stride, long count, int group
 				oracle_cdf97_f_ex_stride_s(sig, sig, h, tmp, N, stride);
 		}
 		free(tmp);
+	}
+}
+
+/* The reference's own calling pattern for a bank of strided signals (the
+ * OpenMP loop its callers write around dwt_cdf97_f_ex_stride_s,
+ * src/libdwt.c:5512-5557): one call of `fn` per signal, in place (L at the
+ * signal's start, H ceil(N/2) samples later), with a per-thread 16-byte
+ * aligned tmp (forward gets tmp + 3, so that the lifting array tmp + 4 the
+ * SSE kernels use is aligned; inverse gets tmp).  `fn` is the forward or
+ * inverse strided function of any library with the reference's signature:
+ * the compiled reference itself (timed as the CPU baseline), or the oracle. */
+typedef void (*oracle_fwd1_fn)(const float *, float *, float *, float *, int, int);
+typedef void (*oracle_inv1_fn)(const float *, const float *, float *, float *, int, int);
+
+void oracle_call_1_batch_s(void *fn, void *base, int N, int stride, long count, int group,
+                           long group_stride, int lane_stride, int inverse, int threads)
+{
+	#pragma omp parallel num_threads(threads) if(threads > 1)
+	{
+		void *raw = malloc(sizeof(float) * (N + 16) + 16);
+		float *tmp = (float *)(((uintptr_t)raw + 15) & ~(uintptr_t)15);
+		#pragma omp for schedule(static)
+		for (long s = 0; s < count; s++) {
+			float *sig = (float *)((char *)base + (s / group) * group_stride + (s % group) * (long)lane_stride);
+			float *h = (float *)((char *)sig + (ptrdiff_t)ceil_div2(N) * stride);
+			if (inverse)
+				((oracle_inv1_fn)fn)(sig, h, sig, tmp, N, stride);
+			else
+				((oracle_fwd1_fn)fn)(sig, sig, h, tmp + 3, N, stride);
+		}
+		free(raw);
 	}
 }
 

@@ -26,10 +26,17 @@ _vp = C.c_void_p
 _i = C.c_int
 
 
+def reference_dir() -> str:
+    """Where the reference checkout lies: $DWT_REFERENCE_DIR, else a directory
+    named ``reference`` beside this repository (it is read, never written)."""
+    d = os.environ.get("DWT_REFERENCE_DIR")
+    return d if d else os.path.abspath(os.path.join(HERE, "..", "..", "reference"))
+
+
 def build(ref: bool = False) -> None:
     """Compile the oracle (and, if asked and its source exists, the reference)."""
     targets = ["oracle"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"REF_DIR={reference_dir()}"] + targets, check=True)
 
 
 def _declare(lib, prefix: str) -> None:
@@ -60,6 +67,7 @@ def lib():
                 getattr(L, f"oracle_{w}_2i_{t}").argtypes = [_vp, _i, _i, _i, _i, _i, _i,
                                                             _i, _i, _i, _i]
         L.oracle_cdf97_1_batch_s.argtypes = [_vp, _i, _i, C.c_long, _i, C.c_long, _i, _i, _i]
+        L.oracle_call_1_batch_s.argtypes = [_vp, _vp, _i, _i, C.c_long, _i, C.c_long, _i, _i, _i]
         L.oracle_test_image_fill_s.argtypes = [_vp, _i, _i, _i, _i, _i]
         L.oracle_max_threads.restype = _i
         _oracle = L

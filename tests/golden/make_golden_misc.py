@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
 
-REF_HEADER = "/root/reference/src/libdwt.h"
+REF_HEADER = os.path.join(O.reference_dir(), "src", "libdwt.h")
 
 
 def api_functions() -> list:

@@ -85,3 +85,49 @@ def test_replay_latencies(env):
     lat = srv.replay(arrival, reqs)
     assert lat.shape == (n,) and np.all(lat > 0) and np.percentile(lat, 99) < 1.0
     srv.close()
+
+
+def test_reserved_arena_serves_without_device_allocation(env):
+    """After dwt_gpu_server_reserve, a replayed mix of sizes, wavelets and
+    directions is served from the reserved arena: no cudaMalloc or
+    cudaHostAlloc of the server during the replay, every tracked result equal
+    to the same transform alone, and the arena empty afterwards."""
+    D, torch = env
+    rng = np.random.default_rng(23)
+    src_big = torch.from_numpy(rng.integers(0, 256, size=(2600, 2600)).astype(np.float32)).cuda()
+    srv = D.Server(budget_bytes=8 << 30, n_streams=4)
+    srv.reserve(4 << 30)
+    st0 = srv.stats()
+    assert st0["arena_bytes"] >= 4 << 30 and st0["completed"] == 0 and st0["bytes_in_use"] == 0
+    n = 240
+    arrival = np.cumsum(rng.exponential(1 / 2000, n))
+    reqs, tracked = [], []
+    for k in range(n):
+        big = k % 16 == 5
+        w = int(rng.integers(1450, 2600)) if big else int(rng.integers(1, 1100))
+        h = int(rng.integers(1450, 2600)) if big else int(rng.integers(1, 1100))
+        wav = str(rng.choice(["cdf97", "cdf53"]))
+        inv = bool(rng.integers(0, 2))
+        j = int(rng.integers(1, 7))
+        src = src_big[:h, :w]
+        if k % 4 == 0:
+            dst = torch.full((h, w), float("nan"), device="cuda")
+            tracked.append((src, dst, wav, inv, j))
+            reqs.append(D.Server.request(src, dst, wav, inv, j, tag=k))
+        else:
+            reqs.append(D.Server.request(src, None, wav, inv, j, tag=k, w=w, h=h))
+    lat = srv.replay(arrival, reqs, timeout_s=120)
+    st1 = srv.stats()
+    assert lat.shape == (n,) and np.all(lat > 0)
+    assert st1["device_allocs"] == st0["device_allocs"], (st0, st1)
+    assert st1["completed"] == n and st1["bytes_in_use"] == 0
+    bad = []
+    for (src, dst, wav, inv, j) in tracked:
+        alone = torch.empty_like(dst)
+        D.transform2_dev(src, alone, wav, inv, j)
+        torch.cuda.synchronize()
+        if not torch.equal(alone, dst):
+            bad.append((tuple(dst.shape), wav, inv, j))
+    assert not bad, bad[:5]
+    assert D.lib().dwt_gpu_sync_check() == 0
+    srv.close()

@@ -2,7 +2,8 @@
 (examples/{simple,simple-double,simple-perf,start,subbands,perf-plot}),
 compiled unchanged against the reference's own header, link against this
 library instead of libdwt.o with no unresolved symbol.  Runs only where the
-reference sources are present (DWT_REFERENCE_DIR); nothing is copied."""
+reference sources are present ($DWT_REFERENCE_DIR, else a `reference`
+directory beside the repository); nothing is copied."""
 import glob
 import os
 import shutil
@@ -10,7 +11,9 @@ import subprocess
 
 import pytest
 
-REF = os.environ.get("DWT_REFERENCE_DIR", "/root/reference")
+from oracle import oracle as O
+
+REF = O.reference_dir()
 EXAMPLES = ["simple", "simple-double", "simple-perf", "start", "subbands", "perf-plot"]
 
 
