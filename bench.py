@@ -139,6 +139,31 @@ def cpu_baseline(img: np.ndarray, threads: int, min_s: float = 10.0, max_s: floa
                  f"{pairs} pairs in {dt:.1f} s")
 
 
+def cpu_configs(threads: int, loops: int = 3) -> dict:
+    """The CPU restatement's rate on every 2D configuration of the benchmark
+    (forward + inverse, best of `loops` as the reference's perf harness
+    measures, src/libdwt.c:8440-8492): the 1024^2 plain drop-in (j = 5) with
+    each wavelet, the 16384^2 image with CDF 5/3, and the 16383 x 16385 odd
+    size with each wavelet; Mpx/s of inner pixels per transform."""
+    from libdwt_gb300 import synth
+    from oracle import oracle as O
+    out = {"cores": threads, "kind": "port", "unit": "Mpx/s (forward + inverse pair)", "loops": loops}
+    cases = [("c0_1024_cdf97_j5", 1024, 1024, "cdf97", 5), ("c0_1024_cdf53_j5", 1024, 1024, "cdf53", 5),
+             ("c1_16384_cdf53_j14", 16384, 16384, "cdf53", 14),
+             ("c1_16383x16385_cdf97_j14", 16383, 16385, "cdf97", 14),
+             ("c1_16383x16385_cdf53_j14", 16383, 16385, "cdf53", 14)]
+    for name, w, h, wav, j in cases:
+        img = synth_image() if (w, h) == (W, H) else synth.image(w, h, seed=0 if w == h else 1)
+        best = float("inf")
+        for _ in range(loops if w * h < 1 << 26 else 1):
+            t = time.perf_counter()
+            f, jj = O.transform2_dense(img, wav, "f", j, 0, "s", threads)
+            O.transform2_dense(f, wav, "i", jj, 0, "s", threads)
+            best = min(best, time.perf_counter() - t)
+        out[name] = round(2 * w * h / best / 1e6, 1)
+    return out
+
+
 def cpu_checks(threads: int, main_img, main_coef, main_rec, checks: dict) -> dict:
     """The checker half of the CPU leg: max and RMS error of every
     configuration's GPU output against the oracle's FP64 transform (the
@@ -182,7 +207,12 @@ def cpu_checks(threads: int, main_img, main_coef, main_rec, checks: dict) -> dic
         t0 = time.perf_counter()
         O.batch_1d_cdf97(bank, n, st, bank.shape[0] * lanes, lanes, gs, 4, False, threads)
         dt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.batch_1d_cdf97(bank, n, st, bank.shape[0] * lanes, lanes, gs, 4, True, threads)
+        dti = time.perf_counter() - t0
         out["c4_cpu_fwd_gsamples_s"] = {"value": round(bank.size / dt / 1e9, 3), "cores": threads, "kind": "port",
+                                        "sample": f"{bank.shape[0] * lanes} signals of {n}"}
+        out["c4_cpu_inv_gsamples_s"] = {"value": round(bank.size / dti / 1e9, 3), "cores": threads, "kind": "port",
                                         "sample": f"{bank.shape[0] * lanes} signals of {n}"}
     return out
 
@@ -286,7 +316,7 @@ def main():
                     help="length of the serving replay in the extras")
     ap.add_argument("--image", type=int, default=16384,
                     help="image side (a smaller case for profiler captures)")
-    ap.add_argument("--only", choices=["c2", "c3", "c4"], default=None,
+    ap.add_argument("--only", choices=["c2", "c3", "c4", "dropin"], default=None,
                     help="run one secondary configuration alone and print its figures "
                          "(for profiler captures)")
     ap.add_argument("--c4-groups", type=int, default=8192, help="signal groups of C4 (8 signals each)")
@@ -316,6 +346,8 @@ def main():
             res = run_signals_extra(D, torch, checks, groups=args.c4_groups)
         elif args.only == "c2":
             res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks)
+        elif args.only == "dropin":
+            res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda())
         else:
             res = run_serve_extra(D, torch, SERVE_SECONDS)
         print(json.dumps({"only": args.only, **res}), flush=True)
@@ -430,11 +462,14 @@ def main():
         from oracle import oracle as O
         threads = O.max_threads()
         mpx, desc = cpu_baseline(img, threads)
-        cpu = {"value": round(mpx, 3), "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": desc}
+        cpu = {"value": round(mpx, 3), "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": desc,
+               "pin": ("the reference itself at accel 9 runs this workload at 1.03x the port's rate (x86, same "
+                       "threads, bit-identical outputs; profiles/cpu_reference_vs_port_x86.md)")}
         D.transform2_dev(src, coef, "cdf97", False, J, 0, sptr)
         D.transform2_dev(coef, rec, "cdf97", True, J, 0, sptr)
         torch.cuda.synchronize()
         errors = cpu_checks(threads, img, coef.cpu().numpy(), rec.cpu().numpy(), checks)
+        cpu["configs"] = cpu_configs(threads)
 
     if rank == 0:
         line = {
@@ -473,6 +508,66 @@ def main():
             "extras": extras,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_dropin_extra(D, torch, src, nd=10):
+    """The drop-in calls themselves on device pointers, in place as the
+    reference's callers use them (synchronous calls): CDF 9/7 forward +
+    inverse of the 16384^2 image, and of a 12000^2 image in a 16384^2 outer
+    frame with zero padding (the OpenCV wrapper's power-of-two padding;
+    Mpx/s of inner pixels)."""
+    from libdwt_gb300 import synth
+    out = {}
+    # the drop-in itself on a device pointer (in place, as the reference's
+    # callers use it; synchronous calls), forward + inverse of 16384^2
+    dimg = src.clone()
+    dp = dimg.data_ptr()
+    for _ in range(2):
+        jd = D.dwt_cdf97_2f_s(dp, W * 4, 4, W, H, W, H, J)
+        D.dwt_cdf97_2i_s(dp, W * 4, 4, W, H, W, H, jd)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(nd):
+        jd = D.dwt_cdf97_2f_s(dp, W * 4, 4, W, H, W, H, J)
+        D.dwt_cdf97_2i_s(dp, W * 4, 4, W, H, W, H, jd)
+    dt = time.perf_counter() - t
+    out["c1_dropin_device_mpx_s"] = round(nd * 2 * W * H / dt / 1e6, 1)
+    out["c1_dropin_device_ms_per_pair"] = round(dt / nd * 1e3, 3)
+    out["c1_dropin_device_roundtrip_max_abs_err"] = float((dimg - src).abs().max().item())
+    del dimg
+    # a sparse frame: a 12000^2 image in a 16384^2 outer frame with zero
+    # padding (the OpenCV wrapper's power-of-two padding), drop-in forward +
+    # inverse in place on the device; Mpx/s of inner pixels
+    sp = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    sp[:12000, :12000] = torch.from_numpy(synth.image(12000, 12000, seed=9)).cuda()
+    spp = sp.data_ptr()
+    for _ in range(2):
+        js = D.dwt_cdf97_2f_s(spp, W * 4, 4, W, H, 12000, 12000, -1, 0, 1)
+        D.dwt_cdf97_2i_s(spp, W * 4, 4, W, H, 12000, 12000, js, 0, 1)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(nd):
+        js = D.dwt_cdf97_2f_s(spp, W * 4, 4, W, H, 12000, 12000, -1, 0, 1)
+        D.dwt_cdf97_2i_s(spp, W * 4, 4, W, H, 12000, 12000, js, 0, 1)
+    dt = time.perf_counter() - t
+    out["c1_sparse_12000_in_16384_dropin_device_mpx_s"] = round(nd * 2 * 12000 * 12000 / dt / 1e6, 1)
+    del sp
+    # the same 12000^2 image as a dense frame (outer = inner), same calls:
+    # the rate the sparse frame is compared with, per inner pixel
+    de = torch.from_numpy(synth.image(12000, 12000, seed=9)).cuda()
+    dep = de.data_ptr()
+    for _ in range(2):
+        js = D.dwt_cdf97_2f_s(dep, 12000 * 4, 4, 12000, 12000, 12000, 12000, -1)
+        D.dwt_cdf97_2i_s(dep, 12000 * 4, 4, 12000, 12000, 12000, 12000, js)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(nd):
+        js = D.dwt_cdf97_2f_s(dep, 12000 * 4, 4, 12000, 12000, 12000, 12000, -1)
+        D.dwt_cdf97_2i_s(dep, 12000 * 4, 4, 12000, 12000, 12000, 12000, js)
+    dt = time.perf_counter() - t
+    out["c1_dense_12000_dropin_device_mpx_s"] = round(nd * 2 * 12000 * 12000 / dt / 1e6, 1)
+    del de
+    return out
 
 
 def run_e2e(D, torch, img, args, ws):
@@ -532,6 +627,7 @@ def run_extras(D, torch, stream, sptr, checks: dict):
         ms = timed(lambda: D.transform2_dev(osrc[:, :ow], odst, wav, False, J, 0, sptr), 10)
         out[f"{wav}_fwd_16383x16385_mpx_s"] = round(ow * oh / ms / 1e3, 1)
     del osrc, odst
+    out.update(run_dropin_extra(D, torch, src))
     # plain drop-in latency, 1024^2 j=5 on a host image (forward + inverse)
     small = synth.image(1024, 1024, seed=2)
     t = time.perf_counter()
@@ -692,6 +788,7 @@ def run_signals_extra(D, torch, checks: dict, groups=8192, n=4097, lanes=8):
         inv()
     ti = (time.perf_counter() - t0) / reps
     samples = groups * lanes * n
+    percall = c4_per_call(D, torch, x, n, lanes)
     # one forward pass on a slice, checked in the CPU leg
     part = x[:64].copy()
     dpart = torch.from_numpy(part).cuda()
@@ -701,7 +798,47 @@ def run_signals_extra(D, torch, checks: dict, groups=8192, n=4097, lanes=8):
     return {"c4_signals": count, "c4_n": n, "c4_fwd_ms": round(tf * 1e3, 3), "c4_inv_ms": round(ti * 1e3, 3),
             "c4_fwd_gsamples_s": round(samples / tf / 1e9, 2), "c4_inv_gsamples_s": round(samples / ti / 1e9, 2),
             "c4_fwd_frac_alg": round(8 * samples / tf / 1e9 / peak, 4),
-            "c4_inv_frac_alg": round(8 * samples / ti / 1e9 / peak, 4)}
+            "c4_inv_frac_alg": round(8 * samples / ti / 1e9 / peak, 4), **percall}
+
+
+def c4_per_call(D, torch, bank, n, lanes, n_groups=512, threads=16):
+    """The reference's own calling pattern for the signal bank, against this
+    library: `threads` host threads, each calling the drop-in
+    dwt_cdf97_f_ex_stride_s once per signal of its share (in place, L at the
+    signal's start, H ceil(N/2) samples later, element stride 32 B), on the
+    first `n_groups` groups of the bank -- in the reference's host memory
+    (malloc'ed) and on a device copy.  Reports Gsamples/s and microseconds
+    per call, beside the batched launch's figures."""
+    import ctypes as C
+    import threading
+    L = D.lib()
+    f = L.dwt_cdf97_f_ex_stride_s
+    part = np.ascontiguousarray(bank[:n_groups]).copy()
+    dev = torch.from_numpy(part).cuda()
+    count = n_groups * lanes
+    st, gs = lanes * 4, n * lanes * 4
+    off_h = ((n + 1) // 2) * st
+    out = {}
+    for where, base in (("host", part.ctypes.data), ("device", dev.data_ptr())):
+        def work(k0, k1):
+            for s in range(k0, k1):
+                a = base + (s // lanes) * gs + (s % lanes) * 4
+                f(a, a, a + off_h, None, n, st)
+        f(base, base, base + off_h, None, n, st)  # first call outside the timing
+        torch.cuda.synchronize()
+        ths = [threading.Thread(target=work, args=(count * t // threads, count * (t + 1) // threads))
+               for t in range(threads)]
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        dt = time.perf_counter() - t0
+        out[f"c4_dropin_per_call_{where}_gsamples_s"] = round(count * n / dt / 1e9, 4)
+        out[f"c4_dropin_per_call_{where}_us"] = round(dt / count * threads * 1e6, 1)
+    out["c4_dropin_per_call_sample"] = (f"{count} signals of {n} (the first {n_groups} groups), {threads} host "
+                                        f"threads, one dwt_cdf97_f_ex_stride_s call per signal")
+    return out
 
 
 def run_batch_extra(D, torch, stream, sptr, checks: dict, n_images=4096, j=4):

@@ -709,6 +709,244 @@ static int pipelined_inverse(Lane &c, int wavelet, char *host, long long sx, int
     return set_error(check_device_error(c));
 }
 
+// ------------------------------------------------ in place on device frames
+
+// A dense device frame transformed in place (the reference's own calling
+// convention, src/libdwt.h:491-502) without staging the whole frame.  Only
+// level 0 -- the last level of the inverse -- has an in-place hazard: its
+// tiles write the three detail quadrants (top right, bottom left, bottom
+// right) where other tiles still read their input.  Every coarser level only
+// reads the top-left quadrant and the LL scratch and writes the top-left
+// quadrant, which level 0 no longer reads (forward) or does not touch until
+// they are done (inverse).  So:
+//   forward: level 0 reads the frame and writes its three detail bands to a
+//            staging frame T (LL1 to scratch); then, on a second stream, the
+//            three quadrants are copied from T into the frame while levels
+//            1 .. J-1 run on the first and write the top-left quadrant;
+//   inverse: the three detail quadrants are copied from the frame into T on
+//            a second stream while levels J .. 2 read the top-left quadrant;
+//            level 1 then reads LL1 and the details from T and writes the
+//            whole frame.
+// Extra traffic: 6 bytes per pixel (three quarters of the frame read and
+// written once) instead of 8 for a staged copy of the whole frame, and the
+// copy overlaps the coarser, latency-bound levels.
+constexpr long long kInPlaceMinPixels = 1LL << 20;
+
+// DWT_GPU_SPARSE_FUSED=0 keeps sparse frames on the per-line sequence.
+static bool sparse_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_SPARSE_FUSED");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+// DWT_GPU_INPLACE=0 stages the whole frame instead (the general path).
+static bool inplace_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_INPLACE");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+static bool inplace_device_ok(const void *ptr, long long sx_bytes, int W, int H, int J)
+{
+    return J >= 2 && (long long)W * H >= kInPlaceMinPixels && (sx_bytes % 16) == 0 &&
+           (reinterpret_cast<uintptr_t>(ptr) & 15) == 0 && coarse_level(W, H, J) >= 1;
+}
+
+static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long long sx_bytes, int W, int H, int J)
+{
+    cudaStream_t s = c.stream, s2 = c.s_in;
+    const long long Fp = sx_bytes / 4;
+    const long long P = align_up(W, 32);
+    const int ws = (W + 1) / 2, hs = (H + 1) / 2;
+    Buf T(size_t(P) * H * 4 + 256, s);
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(W, H, J, &p0, &p1);
+    Buf scratch(sf * 4 + 256, s);
+    if (!T.p || (sf && !scratch.p)) return set_error(DWT_GPU_ENOMEM);
+    float *buf[2];
+    long long p[2];
+    scratch_frames(W, H, J, scratch.f(), buf, p);
+    cudaEvent_t e_start = c.event(0), e_copy = c.event(1);
+    if (!e_start || !e_copy) return set_error(DWT_GPU_ECUDA);
+    // the three detail quadrants between the frame and T (same positions):
+    // the right part of the top rows, then the whole bottom rows
+    auto copy_details = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        if (W > ws) e = launch_copy_rows_dev(dst + ws, dp * 4, src + ws, sp * 4, (W - ws) * 4LL, hs, s2);
+        if (e == cudaSuccess && H > hs)
+            e = launch_copy_rows_dev(dst + hs * dp, dp * 4, src + hs * sp, sp * 4, W * 4LL, H - hs, s2);
+        return e;
+    };
+    if (!inverse) {
+        LevelDesc d = fwd_desc(F, Fp, T.f(), P, W, H, J, 0, buf, p);
+        plan_level(d, 0, false);
+        CK(launch_level(d, wavelet, false, s, c.d_err));
+        CK(cudaEventRecord(e_start, s));
+        CK(cudaStreamWaitEvent(s2, e_start, 0));
+        CK(copy_details(F, Fp, T.f(), P));
+        CK(cudaEventRecord(e_copy, s2));
+        CK(dense_forward_levels(F, Fp, F, Fp, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
+        CK(cudaStreamWaitEvent(s, e_copy, 0));
+    } else {
+        CK(cudaEventRecord(e_start, s));
+        CK(cudaStreamWaitEvent(s2, e_start, 0));
+        CK(copy_details(T.f(), P, F, Fp));
+        CK(cudaEventRecord(e_copy, s2));
+        CK(dense_inverse_levels(F, Fp, F, Fp, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
+        CK(cudaStreamWaitEvent(s, e_copy, 0));
+        LevelDesc d = inv_desc(T.f(), P, F, Fp, W, H, J, 1, buf, p);
+        plan_level(d, 0, true);
+        d.reverse = kAlternateOrder && ((coarse_level(W, H, J) - 1) & 1);
+        CK(launch_level(d, wavelet, true, s, c.d_err));
+    }
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+// ----------------------------------------- sparse frames with zero padding
+
+// An outer ox x oy frame holding an ix x iy inner image (the SIMPLE / SPARSE
+// layouts of src/libdwt.c:8620-8659, and the OpenCV wrapper's padding,
+// src/cvdwt.cpp:149-181), transformed in place with zero padding.  Per level
+// the reference transforms every row of the outer frame over the inner
+// length, then every column, writing H at the OUTER midpoint, and zeroes the
+// rest of the level's frame (src/libdwt.c:6353-6397, 6700-6745).  Everything
+// it computes outside the inner bands is then overwritten or zeroed, so the
+// result is the dense level of the inner frame with its H bands at the outer
+// midpoints, and zeros everywhere no band of any level lands.  The fused
+// level kernel does the large levels that way (level 0 -- the last inverse
+// level -- through the staging frame T, as for dense frames in place); the
+// small ones run the reference's per-line sequence in place, and a last kernel
+// writes the zeros.
+static bool sparse_fast_level(int iw, int ih) { return iw >= 16 && ih >= 16 && (long long)iw * ih > 4096; }
+
+static bool sparse_fast_ok(const void *F, long long Fp, int ox, int oy, int ix, int iy, int J)
+{
+    return J >= 1 && sparse_fast_level(ix, iy) && (Fp % 4) == 0 && (reinterpret_cast<uintptr_t>(F) & 15) == 0 &&
+           ox >= ix && oy >= iy;
+}
+
+static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long long Fp, int ox, int oy, int ix,
+                          int iy, int J)
+{
+    cudaStream_t s = c.stream, s2 = c.s_in;
+    auto cdp = [](int v, int j) { return ceil_div_pow2(v, j); };
+    const long long P = align_up(ox, 32);
+    Buf T(size_t(P) * oy * 4 + 256, s);
+    // LL ping-pong frames as the dense pipeline lays them out; with one level
+    // the forward still stages LL1 in the first of them
+    const int Js = std::max(J, 2);
+    long long p0, p1;
+    const size_t sf = dense_scratch_floats(ix, iy, Js, &p0, &p1);
+    Buf scratch(sf * 4 + 256, s);
+    if (!T.p || !scratch.p) return set_error(DWT_GPU_ENOMEM);
+    float *buf[2];
+    long long p[2];
+    scratch_frames(ix, iy, Js, scratch.f(), buf, p);
+    cudaEvent_t e_start = c.event(0), e_copy = c.event(1);
+    if (!e_start || !e_copy) return set_error(DWT_GPU_ECUDA);
+    // level 0's three detail bands between the frame and T (same positions)
+    const int odx = cdp(ox, 1), ody = cdp(oy, 1);
+    const int lx = (ix + 1) / 2, hx = ix / 2, ly = (iy + 1) / 2, hy = iy / 2;
+    auto copy_details = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        auto rect = [&](int x0, int y0, int w, int h) {
+            if (e == cudaSuccess && w > 0 && h > 0)
+                e = launch_copy_rows_dev(dst + y0 * dp + x0, dp * 4, src + y0 * sp + x0, sp * 4, w * 4LL, h, s2);
+        };
+        rect(odx, 0, hx, ly);   // HL
+        rect(0, ody, lx, hy);   // LH
+        rect(odx, ody, hx, hy); // HH
+        return e;
+    };
+    // tmp of the per-line levels: lines x length of the largest such frame
+    auto line_tmp = [&](int j) { return size_t(std::max(cdp(ox, j), cdp(oy, j))) * std::max(cdp(ox, j), cdp(oy, j)); };
+    if (!inverse) {
+        int jf = 0;  // levels 0 .. jf-1 fused, the rest per line
+        while (jf < J && sparse_fast_level(cdp(ix, jf), cdp(iy, jf))) ++jf;
+        Buf tmp(jf < J ? line_tmp(jf) * 4 + 256 : 256, s);
+        if (!tmp.p) return set_error(DWT_GPU_ENOMEM);
+        for (int j = 0; j < jf; ++j) {
+            LevelDesc d{};
+            d.w = cdp(ix, j);
+            d.h = cdp(iy, j);
+            d.in[0] = j == 0 ? F : buf[(j - 1) % 2];
+            d.in_pitch[0] = j == 0 ? Fp : p[(j - 1) % 2];
+            const bool ll_to_frame = j == jf - 1 && j >= 1;
+            d.out[0] = ll_to_frame ? F : buf[j % 2];
+            d.out_pitch[0] = ll_to_frame ? Fp : p[j % 2];
+            float *base = j == 0 ? T.f() : F;
+            const long long bp = j == 0 ? P : Fp;
+            const int dx = cdp(ox, j + 1), dy = cdp(oy, j + 1);
+            d.out[1] = base + dx;
+            d.out[2] = base + dy * bp;
+            d.out[3] = base + dy * bp + dx;
+            d.out_pitch[1] = d.out_pitch[2] = d.out_pitch[3] = bp;
+            plan_level(d, 0, false);
+            d.reverse = kAlternateOrder && (j & 1);
+            CK(launch_level(d, wavelet, false, s, c.d_err));
+            if (j == 0) {
+                CK(cudaEventRecord(e_start, s));
+                CK(cudaStreamWaitEvent(s2, e_start, 0));
+                CK(copy_details(F, Fp, T.f(), P));
+                CK(cudaEventRecord(e_copy, s2));
+                if (jf == 1)  // LL1 into the frame for the per-line levels
+                    CK(launch_copy_rows_dev(F, Fp * 4, buf[0], p[0] * 4, lx * 4LL, ly, s));
+            }
+        }
+        for (int j = jf; j < J; ++j)
+            CK(sparse_forward_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j + 1), cdp(oy, j + 1), cdp(ix, j),
+                                    cdp(iy, j), 1, wavelet, tmp.f(), s));
+        CK(cudaStreamWaitEvent(s, e_copy, 0));
+        CK(launch_zero_uncovered(F, Fp, ox, oy, ix, iy, J, s));
+    } else {
+        // inverse level j rebuilds LL_{j-1} (cdp(i, j-1)) from LL_j and the
+        // level's details at the outer midpoints cdp(o, j); levels 1 .. jf
+        // fused, J .. jf+1 per line (first)
+        int jf = 0;
+        while (jf < J && sparse_fast_level(cdp(ix, jf), cdp(iy, jf))) ++jf;
+        Buf tmp(jf < J ? line_tmp(jf) * 4 + 256 : 256, s);
+        if (!tmp.p) return set_error(DWT_GPU_ENOMEM);
+        CK(cudaEventRecord(e_start, s));
+        CK(cudaStreamWaitEvent(s2, e_start, 0));
+        CK(copy_details(T.f(), P, F, Fp));
+        CK(cudaEventRecord(e_copy, s2));
+        for (int j = J; j > jf; --j)
+            CK(sparse_inverse_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j - 1), cdp(oy, j - 1), cdp(ix, j - 1),
+                                    cdp(iy, j - 1), 1, wavelet, tmp.f(), s));
+        for (int j = jf; j >= 1; --j) {
+            LevelDesc d{};
+            d.w = cdp(ix, j - 1);
+            d.h = cdp(iy, j - 1);
+            d.in[0] = j == jf ? F : buf[(j - 1) % 2];
+            d.in_pitch[0] = j == jf ? Fp : p[(j - 1) % 2];
+            const float *base = j == 1 ? T.f() : F;
+            const long long bp = j == 1 ? P : Fp;
+            const int sx = cdp(ox, j), sy = cdp(oy, j);
+            d.in[1] = base + sx;
+            d.in[2] = base + sy * bp;
+            d.in[3] = base + sy * bp + sx;
+            d.in_pitch[1] = d.in_pitch[2] = d.in_pitch[3] = bp;
+            d.out[0] = j == 1 ? F : buf[(j - 2) % 2];
+            d.out_pitch[0] = j == 1 ? Fp : p[(j - 2) % 2];
+            plan_level(d, 0, true);
+            d.reverse = kAlternateOrder && ((jf - j) & 1);
+            if (j == 1) CK(cudaStreamWaitEvent(s, e_copy, 0));
+            CK(launch_level(d, wavelet, true, s, c.d_err));
+        }
+        // zero padding of the last level: everything outside the inner image
+        if (ox > ix) CK(cudaMemset2DAsync(F + ix, Fp * 4, 0, size_t(ox - ix) * 4, oy, s));
+        if (oy > iy) CK(cudaMemset2DAsync(F + iy * Fp, Fp * 4, 0, size_t(ix) * 4, oy - iy, s));
+    }
+    return DWT_GPU_OK;
+}
+
 // ------------------------------------------------------------ 2D driver
 
 // Validates a caller frame; returns false (and logs) for layouts the
@@ -788,6 +1026,19 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
         }
     }
 
+    // dense, aligned device frames: in place, staging only level 0's details
+    if (on_device && dense && sy == 4 && inplace_device_ok(ptr, csx, ox, oy, J) && inplace_enabled())
+        return inplace_device(c, wavelet, inverse, static_cast<float *>(ptr), csx, ox, oy, J);
+    // sparse, zero-padded, aligned device frames: in place likewise
+    const bool sparse_fast = !dense && zero_padding && sparse_enabled();
+    if (on_device && sparse_fast && sy == 4 && (csx % 16) == 0 &&
+        sparse_fast_ok(ptr, csx / 4, ox, oy, ix, iy, J)) {
+        const int rc = sparse_inplace(c, wavelet, inverse, static_cast<float *>(ptr), csx / 4, ox, oy, ix, iy, J);
+        if (rc != DWT_GPU_OK) return rc;
+        CK(cudaStreamSynchronize(s));
+        return set_error(check_device_error(c));
+    }
+
     // 1. stage into IN
     Buf in(size_t(P) * oy * 4 + 256, s);
     if (!in.p) return set_error(DWT_GPU_ENOMEM);
@@ -837,6 +1088,12 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
             CK(dense_forward(in.f(), P, out, out_pitch, ox, oy, J, wavelet, scratch.f(), s, c.d_err, 0));
         else
             CK(dense_inverse(in.f(), P, out, out_pitch, ox, oy, J, wavelet, scratch.f(), s, c.d_err, 0));
+    } else if (sparse_fast && sparse_fast_ok(in.f(), P, ox, oy, ix, iy, J)) {
+        // sparse frame with zero padding: fused levels, in place on IN
+        const int rc = sparse_inplace(c, wavelet, inverse, in.f(), P, ox, oy, ix, iy, J);
+        if (rc != DWT_GPU_OK) return rc;
+        out = in.f();
+        out_pitch = P;
     } else {
         // sparse frame: the reference's per-line sequence, in place on IN
         const int lmax = std::max(ox, oy);

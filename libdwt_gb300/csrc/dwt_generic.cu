@@ -194,6 +194,32 @@ __global__ void zero_inverse_kernel(float *base, long long ls, long long es, int
     for (int i = N; i < n_dst; ++i) line[i * es] = 0.0f;
 }
 
+// Zeroes every sample of an outer ox x oy frame that no band of the J
+// forward levels of its ix x iy inner frame occupies: the final state of the
+// reference's sparse forward with zero padding (src/libdwt.c:6377-6397),
+// where each level zeroes its frame outside its four bands and the next level
+// works in the top-left part.  Band samples are neither read nor written.
+__global__ void zero_uncovered_kernel(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, int y0)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = y0 + int(blockIdx.y);
+    if (x >= ox || y >= oy) return;
+    bool covered = false;
+    for (int j = 0; j < J; ++j) {
+        const int odx = ceil_div_pow2(ox, j + 1), ody = ceil_div_pow2(oy, j + 1);
+        const int iw = ceil_div_pow2(ix, j), ih = ceil_div_pow2(iy, j);
+        if (x < odx && y < ody) {
+            if (j == J - 1) covered = x < (iw + 1) / 2 && y < (ih + 1) / 2;
+            continue;  // the next level's frame
+        }
+        const bool in_x = x < (iw + 1) / 2 || (x >= odx && x < odx + iw / 2);
+        const bool in_y = y < (ih + 1) / 2 || (y >= ody && y < ody + ih / 2);
+        covered = in_x && in_y;
+        break;
+    }
+    if (!covered) f[(long long)y * pitch + x] = 0.0f;
+}
+
 // Interleaved channels (pixel = `channels` floats) <-> one compact plane per
 // channel, plane c at planes + c * plane_stride (pitch in floats).
 __global__ void deinterleave_kernel(const unsigned char *src, long long src_pitch, int channels, int w, int h,
@@ -251,6 +277,25 @@ cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long lo
 cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long long spitch, long long width,
                              long long rows, cudaStream_t s)
 {
+    return launch_copy_rows_ctas(dst, dpitch, src, spitch, width, rows, s, 0);
+}
+
+cudaError_t launch_copy_rows_dev(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                 long long rows, cudaStream_t s)
+{
+    // device to device: enough blocks to stream at HBM speed (8 per SM)
+    static const int ctas = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
+        return 8 * sms;
+    }();
+    return launch_copy_rows_ctas(dst, dpitch, src, spitch, width, rows, s, ctas);
+}
+
+cudaError_t launch_copy_rows_ctas(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                  long long rows, cudaStream_t s, int ctas_override)
+{
     if (width <= 0 || rows <= 0) return cudaSuccess;
     if (rows > INT32_MAX) return cudaErrorInvalidValue;
     const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
@@ -263,11 +308,12 @@ cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long 
     // moving 4 x 256 elements of a row per step: enough bytes in flight for
     // the host link, few blocks to wait for free SM slots among the band
     // kernels
-    static const int ctas = [] {
+    static const int host_ctas = [] {
         const char *e = getenv("DWT_GPU_COPY_CTAS");
         const int v = e ? atoi(e) : 0;
         return v > 0 ? v : 64;
     }();
+    const int ctas = ctas_override > 0 ? ctas_override : host_ctas;
     const int gx = int(std::min<long long>((per_row + 1023) / 1024, 16));
     const int gy = int(std::min<long long>(rows, std::max(1, ctas / gx)));
     const dim3 grid(gx, gy);
@@ -321,6 +367,17 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
     scatter_signals_kernel<<<grid_for((long long)N * count, 256), 256, 0, s>>>(
         src, spitch, N, static_cast<unsigned char *>(base), stride, count, group, group_stride,
         lane_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_uncovered(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, cudaStream_t s)
+{
+    if (ox <= 0 || oy <= 0 || J <= 0) return cudaSuccess;
+    // one thread per sample, rows on grid.y (at most 65535 rows per launch)
+    for (int y0 = 0; y0 < oy; y0 += 65535) {
+        const dim3 grid(unsigned(ceil_div(ox, 256)), unsigned(std::min(65535, oy - y0)));
+        zero_uncovered_kernel<<<grid, 256, 0, s>>>(f, pitch, ox, oy, ix, iy, J, y0);
+    }
     return cudaGetLastError();
 }
 

@@ -17,6 +17,12 @@ cudaError_t launch_unpack(const float *src, long long spitch, void *dst, long lo
 // translation services), where it keeps the copy asynchronous to the host.
 cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long long spitch, long long width,
                              long long rows, cudaStream_t s);
+// The same between device frames, with enough blocks for HBM bandwidth (the
+// copy engines move 2D device-to-device copies far slower).
+cudaError_t launch_copy_rows_dev(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                 long long rows, cudaStream_t s);
+cudaError_t launch_copy_rows_ctas(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                  long long rows, cudaStream_t s, int ctas);
 
 // strided signal bank <-> compact rows (one signal per row)
 // Interleaved channels (pixel = `channels` floats, rows src_pitch_bytes
@@ -33,6 +39,11 @@ cudaError_t launch_gather_signals(const void *base, int N, long long stride, lon
 cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, void *base, long long stride,
                                    long long count, int group, long long group_stride,
                                    long long lane_stride, cudaStream_t s);
+
+// Zeroes the samples of an outer ox x oy frame that no band of the J forward
+// levels of its ix x iy inner frame occupies (sparse frames with zero
+// padding); band samples are left alone.
+cudaError_t launch_zero_uncovered(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, cudaStream_t s);
 
 // One level of a sparse frame (outer > inner), in place on a compact frame.
 cudaError_t sparse_forward_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int isx,

@@ -23,6 +23,16 @@ bool tensor_copies_enabled()
     return on;
 }
 
+// Wide inverse units (strip pairs; DWT_GPU_WIDE_INV=1 turns them on).
+bool wide_inverse_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_WIDE_INV");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
 bool pdl_enabled()
 {
     static const bool on = [] {
@@ -70,6 +80,32 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
     }
 }
 
+// The per-level kernel of wide inverse launches: units are strip pairs by
+// segments, every warp with a ring of wide stages.
+template <int NS>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3)
+level_kernel_wide(const LevelDesc D, const Wavelet W, int *err, const __grid_constant__ LevelMaps M)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *ring = units::warp_ring(smem, warp, kWStageFloats);
+    uint64_t *bars = units::warp_bars(smem, warp, kWarpsPerCta, kWStageFloats);
+    units::init_bars(bars, lane);
+    pdl_release();
+    pdl_wait();
+    const bool fast_launch = units::fast_ok<true>(D);
+    const bool maps = D.tmap && (smem_addr(smem) & 127) == 0;
+    const CUtensorMap *mll = maps ? &M.ll : nullptr, *mfr = maps ? &M.frame : nullptr;
+    uint32_t tick = 0;
+    const int n_pairs = (D.n_strips + 1) / 2;
+    const int n = n_pairs * D.n_segs;
+    for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
+        const int q = u / n_pairs;
+        const int pair = u % n_pairs, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
+        if (!units::run_unit_wide<NS>(D, W, pair, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr)) break;
+    }
+}
+
 // The driver's tensor-map encoder (resolved once through the runtime).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
@@ -86,17 +122,16 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// A w x h float region at `base` (pitch in floats) with boxes of
-// kBandRowF x 2; false if the geometry does not qualify (16-byte aligned base
-// and pitch).
-bool encode_band_map(CUtensorMap *m, const float *base, long long w, long long h, long long pitch)
+// A w x h float region at `base` (pitch in floats) with boxes of box_w x 2;
+// false if the geometry does not qualify (16-byte aligned base and pitch).
+bool encode_band_map(CUtensorMap *m, const float *base, long long w, long long h, long long pitch, int box_w)
 {
     const auto enc = tensor_map_encoder();
     if (!enc || !base || w <= 0 || h <= 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0 || (pitch & 3) != 0)
         return false;
     cuuint64_t dims[2] = {cuuint64_t(w), cuuint64_t(h)};
     cuuint64_t strides[1] = {cuuint64_t(pitch) * 4};
-    cuuint32_t box[2] = {cuuint32_t(kBandRowF), 2};
+    cuuint32_t box[2] = {cuuint32_t(box_w), 2};
     cuuint32_t es[2] = {1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -106,14 +141,22 @@ bool encode_band_map(CUtensorMap *m, const float *base, long long w, long long h
 // Tensor maps of an inverse level: LL from in[0], and the frame the other
 // three bands live in (HL at +ws, LH at +hs rows, HH at both), when the
 // bands sit in one frame as the level pipeline lays them out.
-bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M)
+bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w)
 {
     if (d.rows_only || d.h < 2 || d.w < 2) return false;
     const long long ws = (d.w + 1) / 2, hs = (d.h + 1) / 2, p = d.in_pitch[2];
     if (d.in_pitch[1] != p || d.in_pitch[3] != p) return false;
     const float *frame = d.in[2] - hs * p;
     if (d.in[1] != frame + ws || d.in[3] != frame + hs * p + ws) return false;
-    return encode_band_map(&M.ll, d.in[0], ws, hs, d.in_pitch[0]) && encode_band_map(&M.frame, frame, d.w, d.h, p);
+    return encode_band_map(&M.ll, d.in[0], ws, hs, d.in_pitch[0], box_w) &&
+           encode_band_map(&M.frame, frame, d.w, d.h, p, box_w);
+}
+
+// Whether an inverse level runs as wide units: 2D levels at least four
+// strips wide.
+bool wide_inverse_level(const LevelDesc &d)
+{
+    return wide_inverse_enabled() && !d.rows_only && d.h > 1 && d.n_strips >= 4;
 }
 
 template <int NS, bool INV>
@@ -128,7 +171,18 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
     LevelMaps M;
     memset(&M, 0, sizeof(M));
     LevelDesc dd = d;
-    dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M)) ? 1 : 0;
+    if (INV && wide_inverse_level(d)) {
+        static const cudaError_t configured_w =
+            cudaFuncSetAttribute(level_kernel_wide<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWSmemBytes);
+        if (configured_w != cudaSuccess) return configured_w;
+        dd.wide = 1;
+        dd.tmap = (tensor_copies_enabled() && encode_inverse_maps(d, M, kWBandRowF)) ? 1 : 0;
+        const int pair_units = (d.n_strips + 1) / 2 * d.n_segs;
+        return launch_pdl(level_kernel_wide<NS>, dim3(ceil_div(pair_units, kWarpsPerCta)), dim3(kWarpsPerCta * 32),
+                          kWSmemBytes, stream, dd, W, err, M);
+    }
+    dd.wide = 0;
+    dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M, kBandRowF)) ? 1 : 0;
     return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W, err,
                       M);
 }
@@ -144,6 +198,7 @@ namespace {
 // 1024 row pairs down.
 constexpr int kSegsForward = 176;
 constexpr int kSegsInverse = 88;
+constexpr int kSegsInverseWide = 128;
 constexpr int kSegsInverseSmall = 128;
 constexpr int kSmallPairs = 1024;
 // Below kSmallPairs the levels are latency-bound: segments as short as 2
@@ -174,10 +229,12 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
         } else {
             static const int segs_f = std::max(1, env_int("DWT_GPU_SEGS_FWD", kSegsForward));
             static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
+            static const int segs_iw = std::max(1, env_int("DWT_GPU_SEGS_INV_WIDE", kSegsInverseWide));
+            const bool wide = inverse && wide_inverse_enabled() && !d.rows_only && d.n_strips >= 4;
             if (!inverse)
                 seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : kSegMinSmall);
             else if (npairs > kSmallPairs)
-                seg = std::max(ceil_div(npairs, segs_i), 4);
+                seg = std::max(ceil_div(npairs, wide ? segs_iw : segs_i), 4);
             else
                 seg = std::max(ceil_div(npairs, kSegsInverseSmall), kSegMinSmall);
         }

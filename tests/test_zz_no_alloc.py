@@ -196,6 +196,9 @@ _FRESH = textwrap.dedent("""
     for (w, h, wav) in ((2048, 2048, D.CDF97), (1500, 999, D.CDF53), (2047, 1023, D.CDF97)):
         j = f(wav, 0, src.data_ptr(), 8192, dst.data_ptr(), 8192, w, h, -1, 0, None)
         assert j > 0
+        # calls share the fixed array: the next one may start only when this
+        # one is done (the two streams are not ordered otherwise)
+        torch.cuda.synchronize()
         assert f(wav, 1, dst.data_ptr(), 8192, back.data_ptr(), 8192, w, h, j, 0,
                  C.c_void_p(side.cuda_stream)) == j
         side.synchronize()
