@@ -316,7 +316,8 @@ def main():
                     help="length of the serving replay in the extras")
     ap.add_argument("--image", type=int, default=16384,
                     help="image side (a smaller case for profiler captures)")
-    ap.add_argument("--only", choices=["c2", "c3", "c4", "dropin"], default=None,
+    ap.add_argument("--dropin-reps", type=int, default=10, help="timed pairs of each drop-in extra")
+    ap.add_argument("--only", choices=["c2", "c3", "c4", "dropin", "sparse"], default=None,
                     help="run one secondary configuration alone and print its figures "
                          "(for profiler captures)")
     ap.add_argument("--c4-groups", type=int, default=8192, help="signal groups of C4 (8 signals each)")
@@ -347,7 +348,9 @@ def main():
         elif args.only == "c2":
             res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks)
         elif args.only == "dropin":
-            res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda())
+            res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda(), args.dropin_reps)
+        elif args.only == "sparse":
+            res = run_dropin_extra(D, torch, None, args.dropin_reps, parts=("sparse",))
         else:
             res = run_serve_extra(D, torch, SERVE_SECONDS)
         print(json.dumps({"only": args.only, **res}), flush=True)
@@ -510,13 +513,23 @@ def main():
         print(json.dumps(line), flush=True)
 
 
-def run_dropin_extra(D, torch, src, nd=10):
+def run_dropin_extra(D, torch, src, nd=10, parts=("dense", "sparse", "dense12000")):
     """The drop-in calls themselves on device pointers, in place as the
     reference's callers use them (synchronous calls): CDF 9/7 forward +
     inverse of the 16384^2 image, and of a 12000^2 image in a 16384^2 outer
     frame with zero padding (the OpenCV wrapper's power-of-two padding;
     Mpx/s of inner pixels)."""
-    from libdwt_gb300 import synth
+    out = {}
+    if "dense" in parts:
+        out.update(_dropin_dense(D, torch, src, nd))
+    if "sparse" in parts:
+        out.update(_dropin_sparse(D, torch, nd))
+    if "dense12000" in parts:
+        out.update(_dropin_dense12000(D, torch, nd))
+    return out
+
+
+def _dropin_dense(D, torch, src, nd):
     out = {}
     # the drop-in itself on a device pointer (in place, as the reference's
     # callers use it; synchronous calls), forward + inverse of 16384^2
@@ -535,6 +548,12 @@ def run_dropin_extra(D, torch, src, nd=10):
     out["c1_dropin_device_ms_per_pair"] = round(dt / nd * 1e3, 3)
     out["c1_dropin_device_roundtrip_max_abs_err"] = float((dimg - src).abs().max().item())
     del dimg
+    return out
+
+
+def _dropin_sparse(D, torch, nd):
+    from libdwt_gb300 import synth
+    out = {}
     # a sparse frame: a 12000^2 image in a 16384^2 outer frame with zero
     # padding (the OpenCV wrapper's power-of-two padding), drop-in forward +
     # inverse in place on the device; Mpx/s of inner pixels
@@ -552,6 +571,12 @@ def run_dropin_extra(D, torch, src, nd=10):
     dt = time.perf_counter() - t
     out["c1_sparse_12000_in_16384_dropin_device_mpx_s"] = round(nd * 2 * 12000 * 12000 / dt / 1e6, 1)
     del sp
+    return out
+
+
+def _dropin_dense12000(D, torch, nd):
+    from libdwt_gb300 import synth
+    out = {}
     # the same 12000^2 image as a dense frame (outer = inner), same calls:
     # the rate the sparse frame is compared with, per inner pixel
     de = torch.from_numpy(synth.image(12000, 12000, seed=9)).cuda()

@@ -900,11 +900,42 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
                     CK(launch_copy_rows_dev(F, Fp * 4, buf[0], p[0] * 4, lx * 4LL, ly, s));
             }
         }
-        for (int j = jf; j < J; ++j)
-            CK(sparse_forward_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j + 1), cdp(oy, j + 1), cdp(ix, j),
-                                    cdp(iy, j), 1, wavelet, tmp.f(), s));
+        if (jf < J && sparse_tail_smem(ox, oy, jf) <= kSparseTailSmem) {
+            CK(launch_sparse_tail(false, F, Fp, ox, oy, ix, iy, jf, J, wavelet, s));
+        } else {
+            for (int j = jf; j < J; ++j)
+                CK(sparse_forward_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j + 1), cdp(oy, j + 1), cdp(ix, j),
+                                        cdp(iy, j), 1, wavelet, tmp.f(), s));
+        }
         CK(cudaStreamWaitEvent(s, e_copy, 0));
-        CK(launch_zero_uncovered(F, Fp, ox, oy, ix, iy, J, s));
+        // zeros where no band of the fused levels lands (the per-line levels
+        // zero their own frames): per fused level, the parts of its frame
+        // outside its four bands and outside the next level's frame
+        ZeroRects R{};
+        auto add = [&](int x0, int y0, int w, int h) {
+            if (w <= 0 || h <= 0 || R.n >= kMaxZeroRects) return;
+            R.x0[R.n] = x0;
+            R.y0[R.n] = y0;
+            R.w[R.n] = w;
+            R.first_row[R.n] = R.total_rows;
+            R.total_rows += h;
+            R.n++;
+        };
+        for (int j = 0; j < jf; ++j) {
+            const int ow = cdp(ox, j), oh = cdp(oy, j), dx = cdp(ox, j + 1), dy = cdp(oy, j + 1);
+            const int iw = cdp(ix, j), ih = cdp(iy, j);
+            const int lxj = (iw + 1) / 2, hxj = iw / 2, lyj = (ih + 1) / 2, hyj = ih / 2;
+            add(lxj, dy, dx - lxj, oh - dy);             // between the L and H columns, below the next frame
+            add(dx + hxj, 0, ow - dx - hxj, oh);         // right of the H columns
+            add(dx, lyj, hxj, dy - lyj);                 // H columns, between the L and H rows
+            add(0, dy + hyj, lxj, oh - dy - hyj);        // L columns, below the H rows
+            add(dx, dy + hyj, hxj, oh - dy - hyj);       // H columns, below the H rows
+            if (j == J - 1) {                            // the last level's frame around LL_J
+                add(lxj, 0, dx - lxj, dy);
+                add(0, lyj, lxj, dy - lyj);
+            }
+        }
+        CK(launch_zero_rects(F, Fp, R, s));
     } else {
         // inverse level j rebuilds LL_{j-1} (cdp(i, j-1)) from LL_j and the
         // level's details at the outer midpoints cdp(o, j); levels 1 .. jf
@@ -917,9 +948,13 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
         CK(cudaStreamWaitEvent(s2, e_start, 0));
         CK(copy_details(T.f(), P, F, Fp));
         CK(cudaEventRecord(e_copy, s2));
-        for (int j = J; j > jf; --j)
-            CK(sparse_inverse_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j - 1), cdp(oy, j - 1), cdp(ix, j - 1),
-                                    cdp(iy, j - 1), 1, wavelet, tmp.f(), s));
+        if (jf < J && sparse_tail_smem(ox, oy, jf) <= kSparseTailSmem) {
+            CK(launch_sparse_tail(true, F, Fp, ox, oy, ix, iy, jf, J, wavelet, s));
+        } else {
+            for (int j = J; j > jf; --j)
+                CK(sparse_inverse_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j - 1), cdp(oy, j - 1),
+                                        cdp(ix, j - 1), cdp(iy, j - 1), 1, wavelet, tmp.f(), s));
+        }
         for (int j = jf; j >= 1; --j) {
             LevelDesc d{};
             d.w = cdp(ix, j - 1);
@@ -941,8 +976,16 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
             CK(launch_level(d, wavelet, true, s, c.d_err));
         }
         // zero padding of the last level: everything outside the inner image
-        if (ox > ix) CK(cudaMemset2DAsync(F + ix, Fp * 4, 0, size_t(ox - ix) * 4, oy, s));
-        if (oy > iy) CK(cudaMemset2DAsync(F + iy * Fp, Fp * 4, 0, size_t(ix) * 4, oy - iy, s));
+        ZeroRects R{};
+        if (ox > ix) {
+            R.x0[R.n] = ix, R.y0[R.n] = 0, R.w[R.n] = ox - ix, R.first_row[R.n] = R.total_rows;
+            R.total_rows += oy, R.n++;
+        }
+        if (oy > iy) {
+            R.x0[R.n] = 0, R.y0[R.n] = iy, R.w[R.n] = ix, R.first_row[R.n] = R.total_rows;
+            R.total_rows += oy - iy, R.n++;
+        }
+        CK(launch_zero_rects(F, Fp, R, s));
     }
     return DWT_GPU_OK;
 }

@@ -130,21 +130,17 @@ __device__ __forceinline__ void line_scale(float *x, long long ts, int N, float 
     for (int i = 1; i < N; i += 2) x[i * ts] = fmul(x[i * ts], odd);
 }
 
-// Forward per-line transform in place on a compact frame: line k starts at
-// base + k*ls, samples es apart.  Reads N samples, writes L to [0, ceil(N/2))
-// and H to [hoff, hoff + floor(N/2)).  One thread per line.
-__global__ void lines_forward_kernel(float *base, long long ls, long long es, int nlines, int N,
-                                     int hoff, float *tmp, const Wavelet W)
+// Forward transform of one line in place: reads N samples (es apart),
+// writes L to [0, ceil(N/2)) and H to [hoff, hoff + floor(N/2)); x is the
+// line's working copy, ts floats between its samples.
+__device__ __forceinline__ void line_forward_one(float *line, long long es, int N, int hoff, float *x, long long ts,
+                                                 const Wavelet &W)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nlines || N <= 0) return;
-    float *line = base + k * ls;
+    if (N <= 0) return;
     if (N == 1) {
         line[0] = fmul(line[0], W.n1_fwd);
         return;
     }
-    float *x = tmp + k;
-    const long long ts = nlines;
     for (int i = 0; i < N; ++i) x[i * ts] = line[i * es];
     for (int s = 0; s < W.nsteps; ++s) line_step(x, ts, N, (s & 1) ? 0 : 1, W.c[s]);
     line_scale(x, ts, N, W.zeta_e, W.zeta_o);
@@ -152,20 +148,16 @@ __global__ void lines_forward_kernel(float *base, long long ls, long long es, in
     for (int i = 0; 2 * i + 1 < N; ++i) line[(hoff + i) * es] = x[(2 * i + 1) * ts];
 }
 
-// Inverse per-line transform: L from [0, ceil(N/2)), H from [hoff, ...),
+// Inverse transform of one line: L from [0, ceil(N/2)), H from [hoff, ...),
 // result to [0, N).
-__global__ void lines_inverse_kernel(float *base, long long ls, long long es, int nlines, int N,
-                                     int hoff, float *tmp, const Wavelet W)
+__device__ __forceinline__ void line_inverse_one(float *line, long long es, int N, int hoff, float *x, long long ts,
+                                                 const Wavelet &W)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nlines || N <= 0) return;
-    float *line = base + k * ls;
+    if (N <= 0) return;
     if (N == 1) {
         line[0] = fmul(line[0], W.n1_inv);
         return;
     }
-    float *x = tmp + k;
-    const long long ts = nlines;
     for (int i = 0; 2 * i < N; ++i) x[(2 * i) * ts] = line[i * es];
     for (int i = 0; 2 * i + 1 < N; ++i) x[(2 * i + 1) * ts] = line[(hoff + i) * es];
     line_scale(x, ts, N, W.zeta_o, W.zeta_e);
@@ -173,16 +165,39 @@ __global__ void lines_inverse_kernel(float *base, long long ls, long long es, in
     for (int i = 0; i < N; ++i) line[i * es] = x[i * ts];
 }
 
+// Per-line transforms in place on a compact frame: line k starts at
+// base + k*ls, samples es apart; one thread per line, the lines' working
+// copies interleaved in tmp so the threads of a warp coalesce.
+__global__ void lines_forward_kernel(float *base, long long ls, long long es, int nlines, int N,
+                                     int hoff, float *tmp, const Wavelet W)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines) return;
+    line_forward_one(base + k * ls, es, N, hoff, tmp + k, nlines, W);
+}
+
+__global__ void lines_inverse_kernel(float *base, long long ls, long long es, int nlines, int N,
+                                     int hoff, float *tmp, const Wavelet W)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlines) return;
+    line_inverse_one(base + k * ls, es, N, hoff, tmp + k, nlines, W);
+}
+
 // Zero padding of a forward level (dwt_zero_padding_f_stride_s): per line,
 // zero L samples [ceil(N/2), nL) and H samples [floor(N/2), nH) from hoff.
+__device__ __forceinline__ void zero_forward_one(float *line, long long es, int N, int nL, int nH, int hoff)
+{
+    for (int i = (N + 1) / 2; i < nL; ++i) line[i * es] = 0.0f;
+    for (int i = N / 2; i < nH; ++i) line[(hoff + i) * es] = 0.0f;
+}
+
 __global__ void zero_forward_kernel(float *base, long long ls, long long es, int nlines, int N, int nL,
                                     int nH, int hoff)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nlines || (nL == 0 && nH == 0)) return;
-    float *line = base + k * ls;
-    for (int i = (N + 1) / 2; i < nL; ++i) line[i * es] = 0.0f;
-    for (int i = N / 2; i < nH; ++i) line[(hoff + i) * es] = 0.0f;
+    zero_forward_one(base + k * ls, es, N, nL, nH, hoff);
 }
 
 // Zero padding of an inverse level (dwt_zero_padding_i_stride_s).
@@ -194,30 +209,70 @@ __global__ void zero_inverse_kernel(float *base, long long ls, long long es, int
     for (int i = N; i < n_dst; ++i) line[i * es] = 0.0f;
 }
 
-// Zeroes every sample of an outer ox x oy frame that no band of the J
-// forward levels of its ix x iy inner frame occupies: the final state of the
-// reference's sparse forward with zero padding (src/libdwt.c:6377-6397),
-// where each level zeroes its frame outside its four bands and the next level
-// works in the top-left part.  Band samples are neither read nor written.
-__global__ void zero_uncovered_kernel(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, int y0)
+// The per-line levels of a sparse frame in one CTA: the level frame of the
+// first of them (ox0 x oy0 samples of f, pitch in floats) is brought into
+// shared memory, every level runs the reference's sequence there (row pass
+// over the outer rows, column pass over the outer columns, zero padding;
+// inverse: the same with the inverse line transform), separated by block
+// barriers, and the frame goes back.  Forward levels j0 .. j1-1, inverse
+// levels j1 .. j0+1 (j0 < j1), sizes by ceil_div_pow2 of the outer and inner
+// sizes of level 0.
+template <bool INV>
+__global__ void __launch_bounds__(512) sparse_tail_kernel(float *f, long long pitch, int ox, int oy, int ix, int iy,
+                                                          int j0, int j1, const Wavelet W)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = y0 + int(blockIdx.y);
-    if (x >= ox || y >= oy) return;
-    bool covered = false;
-    for (int j = 0; j < J; ++j) {
-        const int odx = ceil_div_pow2(ox, j + 1), ody = ceil_div_pow2(oy, j + 1);
-        const int iw = ceil_div_pow2(ix, j), ih = ceil_div_pow2(iy, j);
-        if (x < odx && y < ody) {
-            if (j == J - 1) covered = x < (iw + 1) / 2 && y < (ih + 1) / 2;
-            continue;  // the next level's frame
+    extern __shared__ float sh[];
+    const int fx = ceil_div_pow2(ox, j0), fy = ceil_div_pow2(oy, j0);
+    const int ps = fx | 1;  // odd pitch: the lines of a column pass fall in different banks
+    float *S = sh, *T = sh + ps * fy;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int k = tid; k < fx * fy; k += nt) S[(k / fx) * ps + k % fx] = f[(long long)(k / fx) * pitch + k % fx];
+    __syncthreads();
+    for (int step = 0; step < j1 - j0; ++step) {
+        if (!INV) {
+            const int j = j0 + step;
+            const int osx = ceil_div_pow2(ox, j), osy = ceil_div_pow2(oy, j);
+            const int odx = ceil_div_pow2(ox, j + 1), ody = ceil_div_pow2(oy, j + 1);
+            const int isx = ceil_div_pow2(ix, j), isy = ceil_div_pow2(iy, j);
+            for (int k = tid; k < osy; k += nt) line_forward_one(S + k * ps, 1, isx, odx, T + k, osy, W);
+            __syncthreads();
+            for (int k = tid; k < osx; k += nt) line_forward_one(S + k, ps, isy, ody, T + k, osx, W);
+            __syncthreads();
+            for (int k = tid; k < osy; k += nt) zero_forward_one(S + k * ps, 1, isx, odx, osx - odx, odx);
+            __syncthreads();
+            for (int k = tid; k < osx; k += nt) zero_forward_one(S + k, ps, isy, ody, osy - ody, ody);
+            __syncthreads();
+        } else {
+            const int j = j1 - step;  // LL_j -> LL_{j-1}
+            const int osx = ceil_div_pow2(ox, j), osy = ceil_div_pow2(oy, j);
+            const int odx = ceil_div_pow2(ox, j - 1), ody = ceil_div_pow2(oy, j - 1);
+            const int idx = ceil_div_pow2(ix, j - 1), idy = ceil_div_pow2(iy, j - 1);
+            for (int k = tid; k < ody; k += nt) line_inverse_one(S + k * ps, 1, idx, osx, T + k, ody, W);
+            __syncthreads();
+            for (int k = tid; k < odx; k += nt) line_inverse_one(S + k, ps, idy, osy, T + k, odx, W);
+            __syncthreads();
+            for (int k = tid; k < ody; k += nt)
+                for (int i = idx; i < odx; ++i) S[k * ps + i] = 0.0f;
+            __syncthreads();
+            for (int k = tid; k < odx; k += nt)
+                for (int i = idy; i < ody; ++i) S[i * ps + k] = 0.0f;
+            __syncthreads();
         }
-        const bool in_x = x < (iw + 1) / 2 || (x >= odx && x < odx + iw / 2);
-        const bool in_y = y < (ih + 1) / 2 || (y >= ody && y < ody + ih / 2);
-        covered = in_x && in_y;
-        break;
     }
-    if (!covered) f[(long long)y * pitch + x] = 0.0f;
+    for (int k = tid; k < fx * fy; k += nt) f[(long long)(k / fx) * pitch + k % fx] = S[(k / fx) * ps + k % fx];
+}
+
+// Zero fill of a list of rectangles of a frame (pitch in floats): blocks take
+// the rectangles' rows in turn, their threads the row's samples.
+__global__ void zero_rects_kernel(float *f, long long pitch, const ZeroRects R)
+{
+    for (int r = blockIdx.x; r < R.total_rows; r += gridDim.x) {
+        int k = 0;
+        while (k + 1 < R.n && R.first_row[k + 1] <= r) ++k;
+        const int y = R.y0[k] + (r - R.first_row[k]);
+        float *row = f + (long long)y * pitch + R.x0[k];
+        for (int x = threadIdx.x; x < R.w[k]; x += blockDim.x) row[x] = 0.0f;
+    }
 }
 
 // Interleaved channels (pixel = `channels` floats) <-> one compact plane per
@@ -370,14 +425,36 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
     return cudaGetLastError();
 }
 
-cudaError_t launch_zero_uncovered(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, cudaStream_t s)
+size_t sparse_tail_smem(int ox, int oy, int j0)
 {
-    if (ox <= 0 || oy <= 0 || J <= 0) return cudaSuccess;
-    // one thread per sample, rows on grid.y (at most 65535 rows per launch)
-    for (int y0 = 0; y0 < oy; y0 += 65535) {
-        const dim3 grid(unsigned(ceil_div(ox, 256)), unsigned(std::min(65535, oy - y0)));
-        zero_uncovered_kernel<<<grid, 256, 0, s>>>(f, pitch, ox, oy, ix, iy, J, y0);
-    }
+    const int fx = ceil_div_pow2(ox, j0), fy = ceil_div_pow2(oy, j0);
+    return size_t(fx | 1) * fy * 4 + size_t(fx) * fy * 4;
+}
+
+cudaError_t launch_sparse_tail(bool inverse, float *f, long long pitch, int ox, int oy, int ix, int iy, int j0,
+                               int j1, int wavelet, cudaStream_t s)
+{
+    const size_t smem = sparse_tail_smem(ox, oy, j0);
+    if (smem > kSparseTailSmem || j1 <= j0) return cudaErrorInvalidValue;
+    static const cudaError_t cf = cudaFuncSetAttribute(sparse_tail_kernel<false>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSparseTailSmem);
+    static const cudaError_t ci = cudaFuncSetAttribute(sparse_tail_kernel<true>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSparseTailSmem);
+    if (cf != cudaSuccess) return cf;
+    if (ci != cudaSuccess) return ci;
+    const Wavelet W = make_wavelet(wavelet, inverse);
+    if (inverse)
+        sparse_tail_kernel<true><<<1, 512, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+    else
+        sparse_tail_kernel<false><<<1, 512, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_rects(float *f, long long pitch, const ZeroRects &R, cudaStream_t s)
+{
+    if (R.n <= 0 || R.total_rows <= 0) return cudaSuccess;
+    const int grid = std::min(R.total_rows, 152 * 16);
+    zero_rects_kernel<<<grid, 256, 0, s>>>(f, pitch, R);
     return cudaGetLastError();
 }
 

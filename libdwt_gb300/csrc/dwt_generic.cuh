@@ -40,10 +40,23 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
                                    long long count, int group, long long group_stride,
                                    long long lane_stride, cudaStream_t s);
 
-// Zeroes the samples of an outer ox x oy frame that no band of the J forward
-// levels of its ix x iy inner frame occupies (sparse frames with zero
-// padding); band samples are left alone.
-cudaError_t launch_zero_uncovered(float *f, long long pitch, int ox, int oy, int ix, int iy, int J, cudaStream_t s);
+// The per-line levels of a sparse frame with zero padding in one CTA, the
+// frame of level j0 held in shared memory: forward levels j0 .. j1-1 or
+// inverse levels j1 .. j0+1.  Only when sparse_tail_smem(ox, oy, j0) fits
+// kSparseTailSmem (cudaErrorInvalidValue otherwise).
+constexpr size_t kSparseTailSmem = 200 * 1024;
+size_t sparse_tail_smem(int ox, int oy, int j0);
+cudaError_t launch_sparse_tail(bool inverse, float *f, long long pitch, int ox, int oy, int ix, int iy, int j0,
+                               int j1, int wavelet, cudaStream_t s);
+
+// Rectangles of a frame to fill with zeros (at most kMaxZeroRects; the rows
+// of rectangle k are rows first_row[k] .. of the flattened list).
+constexpr int kMaxZeroRects = 128;
+struct ZeroRects {
+    int n, total_rows;
+    int x0[kMaxZeroRects], y0[kMaxZeroRects], w[kMaxZeroRects], first_row[kMaxZeroRects];
+};
+cudaError_t launch_zero_rects(float *f, long long pitch, const ZeroRects &R, cudaStream_t s);
 
 // One level of a sparse frame (outer > inner), in place on a compact frame.
 cudaError_t sparse_forward_level(float *f, long long pitch, int osx, int osy, int odx, int ody, int isx,

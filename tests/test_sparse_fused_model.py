@@ -6,14 +6,16 @@ an inner image and zero padding, the reference's in-place level sequence
   forward: for the fused levels, one dense level of the inner LL band with
            its H bands placed at the OUTER midpoints; the reference's own
            per-line sequence for the remaining small levels on the top-left
-           sub-frame; then zeros wherever no band of any level lands;
+           sub-frame; then zeros in the rectangles of each fused level's
+           frame that none of its bands (nor the next level's frame) covers;
   inverse: the per-line sequence for the small levels first, then dense
            inverse levels reading the H bands at the outer midpoints; then
            zeros outside the inner image.
 
 Both sides are computed by the oracle (bit-exact with the reference), the
-composition by the same steps and the same zero predicate as the GPU code,
-over random geometries, both wavelets."""
+composition by the same steps and the same zero rectangles as the GPU code,
+over random geometries, both wavelets.  The final forward layout is also
+checked against a per-sample band predicate: a band of some level, or zero."""
 import numpy as np
 import pytest
 
@@ -29,7 +31,7 @@ def fast(iw, ih):
 
 
 def covered(x, y, ox, oy, ix, iy, J):
-    """The band predicate of zero_uncovered_kernel."""
+    """Whether a sample holds a band of some level (final layout)."""
     for j in range(J):
         odx, ody = cdp(ox, j + 1), cdp(oy, j + 1)
         iw, ih = cdp(ix, j), cdp(iy, j)
@@ -49,6 +51,21 @@ def band_mask(ox, oy, ix, iy, J):
         for x in range(ox):
             m[y, x] = covered(x, y, ox, oy, ix, iy, J)
     return m
+
+
+def zero_rects(jf, J, ox, oy, ix, iy):
+    """The rectangles sparse_inplace zeroes after the fused forward levels
+    (x0, y0, w, h), as the GPU code lists them."""
+    rects = []
+    for j in range(jf):
+        ow, oh, dx, dy = cdp(ox, j), cdp(oy, j), cdp(ox, j + 1), cdp(oy, j + 1)
+        iw, ih = cdp(ix, j), cdp(iy, j)
+        lx, hx, ly, hy = (iw + 1) // 2, iw // 2, (ih + 1) // 2, ih // 2
+        rects += [(lx, dy, dx - lx, oh - dy), (dx + hx, 0, ow - dx - hx, oh), (dx, ly, hx, dy - ly),
+                  (0, dy + hy, lx, oh - dy - hy), (dx, dy + hy, hx, oh - dy - hy)]
+        if j == J - 1:
+            rects += [(lx, 0, dx - lx, dy), (0, ly, lx, dy - ly)]
+    return [r for r in rects if r[2] > 0 and r[3] > 0]
 
 
 def reference(frame, wav, direction, ox, oy, ix, iy, J):
@@ -86,7 +103,8 @@ def composed_forward(frame, wav, ox, oy, ix, iy, J):
     out[:ll.shape[0], :ll.shape[1]] = ll
     if jf < J:
         sub_frame_levels(out, wav, "f", ox, oy, ix, iy, jf, J)
-    out[~band_mask(ox, oy, ix, iy, J)] = 0.0
+    for (x0, y0, w, h) in zero_rects(jf, J, ox, oy, ix, iy):
+        out[y0:y0 + h, x0:x0 + w] = 0.0
     return out, jf
 
 
@@ -141,6 +159,8 @@ def test_composition_equals_reference_sequence(wav, geom):
         got_f, jf = composed_forward(frame, wav, ox, oy, ix, iy, J)
         assert jf >= 1
         assert np.array_equal(got_f.view(np.uint32), ref_f.view(np.uint32)), (geom, J, "forward")
+        # the final layout: a band or zero everywhere in the outer frame
+        assert not ref_f[~band_mask(ox, oy, ix, iy, J)].any()
         # the inverse of arbitrary coefficients (stale samples everywhere else)
         coef = ref_f.copy()
         coef[~band_mask(ox, oy, ix, iy, J)] = rng.uniform(-9, 9, size=int((~band_mask(ox, oy, ix, iy, J)).sum()))
