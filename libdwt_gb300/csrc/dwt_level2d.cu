@@ -33,6 +33,18 @@ bool wide_inverse_enabled()
     return on;
 }
 
+// Narrowest inverse level (in strips) that runs as wide units
+// (DWT_GPU_WIDE_MIN_STRIPS, default 4).
+int wide_min_strips()
+{
+    static const int n = [] {
+        const char *v = getenv("DWT_GPU_WIDE_MIN_STRIPS");
+        const int k = v ? atoi(v) : 0;
+        return k >= 4 ? k : 4;
+    }();
+    return n;
+}
+
 bool pdl_enabled()
 {
     static const bool on = [] {
@@ -156,7 +168,7 @@ bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w)
 // strips wide.
 bool wide_inverse_level(const LevelDesc &d)
 {
-    return wide_inverse_enabled() && !d.rows_only && d.h > 1 && d.n_strips >= 4;
+    return wide_inverse_enabled() && !d.rows_only && d.h > 1 && d.n_strips >= wide_min_strips();
 }
 
 template <int NS, bool INV>
@@ -230,7 +242,7 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
             static const int segs_f = std::max(1, env_int("DWT_GPU_SEGS_FWD", kSegsForward));
             static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
             static const int segs_iw = std::max(1, env_int("DWT_GPU_SEGS_INV_WIDE", kSegsInverseWide));
-            const bool wide = inverse && wide_inverse_enabled() && !d.rows_only && d.n_strips >= 4;
+            const bool wide = inverse && wide_inverse_enabled() && !d.rows_only && d.n_strips >= wide_min_strips();
             if (!inverse)
                 seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : kSegMinSmall);
             else if (npairs > kSmallPairs)
