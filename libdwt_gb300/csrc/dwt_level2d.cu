@@ -23,28 +23,6 @@ bool tensor_copies_enabled()
     return on;
 }
 
-// Wide inverse units (strip pairs; DWT_GPU_WIDE_INV=1 turns them on).
-bool wide_inverse_enabled()
-{
-    static const bool on = [] {
-        const char *v = getenv("DWT_GPU_WIDE_INV");
-        return v && v[0] == '1';
-    }();
-    return on;
-}
-
-// Narrowest inverse level (in strips) that runs as wide units
-// (DWT_GPU_WIDE_MIN_STRIPS, default 4).
-int wide_min_strips()
-{
-    static const int n = [] {
-        const char *v = getenv("DWT_GPU_WIDE_MIN_STRIPS");
-        const int k = v ? atoi(v) : 0;
-        return k >= 4 ? k : 4;
-    }();
-    return n;
-}
-
 bool pdl_enabled()
 {
     static const bool on = [] {
@@ -89,32 +67,6 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
         const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
         if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr))
             break;
-    }
-}
-
-// The per-level kernel of wide inverse launches: units are strip pairs by
-// segments, every warp with a ring of wide stages.
-template <int NS>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 3)
-level_kernel_wide(const LevelDesc D, const Wavelet W, int *err, const __grid_constant__ LevelMaps M)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float *ring = units::warp_ring(smem, warp, kWStageFloats);
-    uint64_t *bars = units::warp_bars(smem, warp, kWarpsPerCta, kWStageFloats);
-    units::init_bars(bars, lane);
-    pdl_release();
-    pdl_wait();
-    const bool fast_launch = units::fast_ok<true>(D);
-    const bool maps = D.tmap && (smem_addr(smem) & 127) == 0;
-    const CUtensorMap *mll = maps ? &M.ll : nullptr, *mfr = maps ? &M.frame : nullptr;
-    uint32_t tick = 0;
-    const int n_pairs = (D.n_strips + 1) / 2;
-    const int n = n_pairs * D.n_segs;
-    for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
-        const int q = u / n_pairs;
-        const int pair = u % n_pairs, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
-        if (!units::run_unit_wide<NS>(D, W, pair, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr)) break;
     }
 }
 
@@ -164,13 +116,6 @@ bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w)
            encode_band_map(&M.frame, frame, d.w, d.h, p, box_w);
 }
 
-// Whether an inverse level runs as wide units: 2D levels at least four
-// strips wide.
-bool wide_inverse_level(const LevelDesc &d)
-{
-    return wide_inverse_enabled() && !d.rows_only && d.h > 1 && d.n_strips >= wide_min_strips();
-}
-
 template <int NS, bool INV>
 cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
 {
@@ -183,17 +128,6 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
     LevelMaps M;
     memset(&M, 0, sizeof(M));
     LevelDesc dd = d;
-    if (INV && wide_inverse_level(d)) {
-        static const cudaError_t configured_w =
-            cudaFuncSetAttribute(level_kernel_wide<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWSmemBytes);
-        if (configured_w != cudaSuccess) return configured_w;
-        dd.wide = 1;
-        dd.tmap = (tensor_copies_enabled() && encode_inverse_maps(d, M, kWBandRowF)) ? 1 : 0;
-        const int pair_units = (d.n_strips + 1) / 2 * d.n_segs;
-        return launch_pdl(level_kernel_wide<NS>, dim3(ceil_div(pair_units, kWarpsPerCta)), dim3(kWarpsPerCta * 32),
-                          kWSmemBytes, stream, dd, W, err, M);
-    }
-    dd.wide = 0;
     dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M, kBandRowF)) ? 1 : 0;
     return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W, err,
                       M);
@@ -203,20 +137,22 @@ cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
 
 namespace {
 
-// Segment length of a 2D level, measured on the levels of 16384^2 (level
-// kernel times under ncu): the forward is fastest with about 176 segments
-// per level (none shorter than 8 pairs from 1024 row pairs up, 2 below);
-// the inverse with about 88 on large levels and 128 (at least 2 pairs) from
-// 1024 row pairs down.
+// Segment length of a 2D level, measured on 16384^2 (level kernel times and
+// the whole forward + inverse step, CUDA events): the forward is fastest with
+// about 176 segments per level (none shorter than 8 pairs from 1024 row
+// pairs up, 2 below); the inverse with about 256 on large levels (88: inverse
+// level 0 in 0.361 ms, 176: 0.350, 256: 0.342, 384: 0.338, step best at
+// 256) and 128 (at least 2 pairs) from 1024 row pairs down.
 constexpr int kSegsForward = 176;
-constexpr int kSegsInverse = 88;
-constexpr int kSegsInverseWide = 128;
+constexpr int kSegsInverse = 256;
 constexpr int kSegsInverseSmall = 128;
 constexpr int kSmallPairs = 1024;
 // Below kSmallPairs the levels are latency-bound: segments as short as 2
 // pairs (more, shorter units) measured 5 us faster per 16384^2 forward +
 // inverse than a 4-pair minimum.
 constexpr int kSegMinSmall = 2;
+// Shortest forward segment from kSmallPairs row pairs up.
+constexpr int kSegMinForward = 8;
 
 int env_int(const char *name, int dflt)
 {
@@ -241,14 +177,14 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
         } else {
             static const int segs_f = std::max(1, env_int("DWT_GPU_SEGS_FWD", kSegsForward));
             static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
-            static const int segs_iw = std::max(1, env_int("DWT_GPU_SEGS_INV_WIDE", kSegsInverseWide));
-            const bool wide = inverse && wide_inverse_enabled() && !d.rows_only && d.n_strips >= wide_min_strips();
+            static const int segs_is = std::max(1, env_int("DWT_GPU_SEGS_INV_SMALL", kSegsInverseSmall));
+            static const int fwd_min = std::max(1, env_int("DWT_GPU_SEG_MIN_FWD", kSegMinForward));
             if (!inverse)
-                seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? 8 : kSegMinSmall);
+                seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? fwd_min : kSegMinSmall);
             else if (npairs > kSmallPairs)
-                seg = std::max(ceil_div(npairs, wide ? segs_iw : segs_i), 4);
+                seg = std::max(ceil_div(npairs, segs_i), 4);
             else
-                seg = std::max(ceil_div(npairs, kSegsInverseSmall), kSegMinSmall);
+                seg = std::max(ceil_div(npairs, segs_is), kSegMinSmall);
         }
     }
     seg = std::min(seg, std::max(npairs, 1));

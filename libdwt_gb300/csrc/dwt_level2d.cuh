@@ -28,15 +28,6 @@ constexpr int kStageFloats = 640;  // one pipeline stage = 2 row pairs: 4 rows o
 constexpr int kStages = 4;         // pipeline depth per warp (8 row pairs)
 constexpr int kWarpsPerCta = 4;
 constexpr int kSmemBytes = kWarpsPerCta * (kStages * kStageFloats * 4 + kStages * 8);
-// Wide inverse units: a warp takes two neighbouring strips (240 output
-// columns) at once, so every band row of a stage arrives as one 544-byte
-// piece (124 band columns and the halo, rounded to 16 bytes) instead of two
-// of 272: per band a slot of the stage's two band rows, kWBandRowF floats
-// each, slots on 128-byte boundaries.
-constexpr int kWBandRowF = 136;
-constexpr int kWBandSlotF = 288;
-constexpr int kWStageFloats = 4 * kWBandSlotF;
-constexpr int kWSmemBytes = kWarpsPerCta * (kStages * kWStageFloats * 4 + kStages * 8);
 
 // One level of one image.  Forward: in[0] is the interleaved w x h source,
 // out[0..3] receive LL, HL, LH, HH.  Inverse: in[0..3] are LL, HL, LH, HH,
@@ -51,7 +42,6 @@ struct LevelDesc {
     int reverse;   // hand out the segments bottom-up (the previous level ended there)
     int rows_only;
     int tmap;      // inverse: the tensor maps of the launch are valid (set by launch_level)
-    int wide;      // inverse: units are strip pairs (set by launch_level)
     const float *in[4];
     long long in_pitch[4];
     float *out[4];

@@ -792,137 +792,6 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     return okw;
 }
 
-// A wide inverse unit: the interior strip pair (2 * pair, 2 * pair + 1) by
-// segment `seg`, through the warp's private ring with wide stages (band k at
-// slot + k * kWBandSlotF, the row of the stage's pair r at + r * kWBandRowF).
-// The same arithmetic as inverse_unit, per sub-strip s the lanes hold the
-// columns of strip 2 * pair + s: the stage is read sub-strip by sub-strip, and
-// released once both are read.  Interior only (both strips away from the
-// image borders, every band pointer 8-byte aligned); mll / mfr are maps with
-// kWBandRowF x 2 boxes, or null for bulk copies.
-template <int NS>
-__device__ bool inverse_unit_wide(const LevelDesc &D, const Wavelet &W, int pair, int seg, float *ring,
-                                  uint64_t *bars, const CUtensorMap *mll, const CUtensorMap *mfr, uint32_t &tick,
-                                  int lane, int *err)
-{
-    constexpr int LAT = NS / 2;
-    const int w = D.w, h = D.h;
-    const int b = 2 * pair * kStripOut - 4;  // interleaved column of lane 0's first value, sub-strip 0
-    const int bq = b >> 1;
-    const int Lw = (w + 1) >> 1, Hw = w >> 1;
-    const int hs = (h + 1) >> 1;
-    int k0, total, iters;
-    unit_span<NS>(D, seg, k0, total, iters);
-    const int m0 = k0 - LAT;
-
-    // window: band columns [bq, bq + kStripOut + 4) of every band
-    constexpr int kWin = kStripOut + 4;
-    BandIn iLL, iHL, iLH, iHH;
-    iLL.init(D.in[0], D.in_pitch[0], bq, min(kWin, Lw - bq));
-    iHL.init(D.in[1], D.in_pitch[1], bq, min(kWin, Hw - bq));
-    iLH.init(D.in[2], D.in_pitch[2], bq, min(kWin, Lw - bq));
-    iHH.init(D.in[3], D.in_pitch[3], bq, min(kWin, Hw - bq));
-    const uint32_t tx1 = 2 * (iLL.bytes + iHL.bytes + iLH.bytes + iHH.bytes);
-    const bool boxes = mll != nullptr && mfr != nullptr;
-    constexpr uint32_t kBoxBytes = kWBandRowF * 2 * 4;
-
-    const uint32_t t0 = tick;
-    auto slot_of = [&](uint32_t t) { return ring + (t % kStages) * kWStageFloats; };
-    auto bar_of = [&](uint32_t t) { return &bars[t % kStages]; };
-    auto issue = [&](int u) {
-        const uint32_t t = t0 + u;
-        float *slot = slot_of(t);
-        uint64_t *bar = bar_of(t);
-        const int m = m0 + 2 * u;
-        fence_proxy_async_smem();
-        if (boxes && m >= 0 && 2 * m + 3 < h) {
-            mbar_arrive_expect_tx(bar, 4 * kBoxBytes);
-            tma_load_2d(slot, mll, bq - iLL.shift, m, bar);
-            tma_load_2d(slot + kWBandSlotF, mfr, Lw + bq - iHL.shift, m, bar);
-            tma_load_2d(slot + 2 * kWBandSlotF, mfr, bq - iLH.shift, hs + m, bar);
-            tma_load_2d(slot + 3 * kWBandSlotF, mfr, Lw + bq - iHH.shift, hs + m, bar);
-            return;
-        }
-        mbar_arrive_expect_tx(bar, tx1);
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            int ra, rb;
-            pair_rows(m + r, h, ra, rb);
-            const int qa = ra >> 1, qb = rb >> 1;
-            float *sl = slot + r * kWBandRowF;
-            bulk_g2s(sl, iLL.base + qa * iLL.pitch, iLL.bytes, bar);
-            bulk_g2s(sl + kWBandSlotF, iHL.base + qa * iHL.pitch, iHL.bytes, bar);
-            bulk_g2s(sl + 2 * kWBandSlotF, iLH.base + qb * iLH.pitch, iLH.bytes, bar);
-            bulk_g2s(sl + 3 * kWBandSlotF, iHH.base + qb * iHH.pitch, iHH.bytes, bar);
-        }
-    };
-    if (lane == 0)
-        for (int u = 0; u < min(iters, kStages); ++u) issue(u);
-    __syncwarp();
-
-    f2 C[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = pk(W.c[k], W.c[k]);
-    const f2 ZE = pk(W.zeta_e, W.zeta_e), ZO = pk(W.zeta_o, W.zeta_o);
-
-    const bool lane_ok = lane >= 1 && lane <= kLanes - 2;
-    const long long opitch = D.out_pitch[0];
-    float *orow = D.out[0] + b + 4 * lane + (long long)(2 * k0) * opitch;
-    const int last_odd = (h >> 1) - 1;
-
-    f2 o[2][2] = {{0, 0}, {0, 0}}, e1[2][2] = {{0, 0}, {0, 0}}, o1[2][2] = {{0, 0}, {0, 0}},
-       e2[2][2] = {{0, 0}, {0, 0}};
-
-#pragma unroll 1
-    for (int u = 0; u < iters; ++u) {
-        if (!__all_sync(kFull, mbar_wait_bounded(bar_of(t0 + u), ((t0 + u) / kStages) & 1u))) {
-            if (lane == 0) raise_error(err, kErrWaitTimeout);
-            return false;
-        }
-        const float *slot = slot_of(t0 + u);
-#pragma unroll
-        for (int sub = 0; sub < 2; ++sub) {
-            const int d = kStripOut / 2 * sub + 2 * lane;
-            f2 E[4], O[4];
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const float *sl = slot + r * kWBandRowF;
-                E[2 * r] = *reinterpret_cast<const f2 *>(sl + d + iLL.shift);
-                O[2 * r] = *reinterpret_cast<const f2 *>(sl + kWBandSlotF + d + iHL.shift);
-                E[2 * r + 1] = *reinterpret_cast<const f2 *>(sl + 2 * kWBandSlotF + d + iLH.shift);
-                O[2 * r + 1] = *reinterpret_cast<const f2 *>(sl + 3 * kWBandSlotF + d + iHH.shift);
-            }
-            if (sub == 1) {
-                // both halves of the stage are read: refill it kStages ahead
-                __syncwarp();
-                if (lane == 0 && u + kStages < iters) issue(u + kStages);
-            }
-#pragma unroll
-            for (int r = 0; r < 4; ++r) h_inverse2<NS>(E[r], O[r], C, ZE, ZO);
-            float *op = orow + sub * kStripOut;
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int t = 2 * u + r;
-                f2 EvE, OvE, EvO, OvO;
-                v_inverse2<NS>(E[2 * r], E[2 * r + 1], o[sub][0], e1[sub][0], o1[sub][0], e2[sub][0], C, ZE, ZO,
-                               EvE, OvE);
-                v_inverse2<NS>(O[2 * r], O[2 * r + 1], o[sub][1], e1[sub][1], o1[sub][1], e2[sub][1], C, ZE, ZO,
-                               EvO, OvO);
-                if (t >= 2 * LAT && t < total && lane_ok) {
-                    const int p = m0 + t - LAT;
-                    float *q = op + (long long)(2 * (t - 2 * LAT)) * opitch;
-                    *reinterpret_cast<float4 *>(q) = make_float4(f2lo(EvE), f2lo(EvO), f2hi(EvE), f2hi(EvO));
-                    if (p <= last_odd)
-                        *reinterpret_cast<float4 *>(q + opitch) =
-                            make_float4(f2lo(OvE), f2lo(OvO), f2hi(OvE), f2hi(OvO));
-                }
-            }
-        }
-    }
-    tick += iters;
-    return true;
-}
-
 // Whether interior units of a launch may use vector loads and stores: every
 // band pointer and pitch must keep them aligned.
 template <bool INV>
@@ -964,34 +833,14 @@ __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, i
                 : forward_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err);
 }
 
-// A unit of a wide inverse launch: strip pair `pair` by segment `seg`.
-// Interior pairs take the wide path; a pair touching a border (or one left
-// without a partner at the right end) runs its strips as ordinary units.
-template <int NS>
-__device__ __forceinline__ bool run_unit_wide(const LevelDesc &D, const Wavelet &W, int pair, int seg,
-                                              float *ring, uint64_t *bars, uint32_t &tick, int lane, int *err,
-                                              bool fast_launch, const CUtensorMap *mll, const CUtensorMap *mfr)
+// Per-warp ring and barriers inside a CTA's dynamic shared memory.
+__device__ __forceinline__ float *warp_ring(unsigned char *smem, int warp)
 {
-    const int s0 = 2 * pair;
-    const int b0 = s0 * kStripOut - 4;
-    const bool interior = fast_launch && b0 >= 0 && s0 + 1 < D.n_strips && b0 + kStripOut + kStripIn + 2 <= D.w;
-    if (interior) return inverse_unit_wide<NS>(D, W, pair, seg, ring, bars, mll, mfr, tick, lane, err);
-    for (int st = s0; st < min(s0 + 2, D.n_strips); ++st)
-        if (!run_unit<NS, true>(D, W, st, seg, ring, bars, tick, lane, err, fast_launch, nullptr, nullptr))
-            return false;
-    return true;
+    return reinterpret_cast<float *>(smem) + warp * kStages * kStageFloats;
 }
-
-// Per-warp ring and barriers inside a CTA's dynamic shared memory
-// (stage_floats: kStageFloats, or kWStageFloats for wide inverse launches).
-__device__ __forceinline__ float *warp_ring(unsigned char *smem, int warp, int stage_floats = kStageFloats)
+__device__ __forceinline__ uint64_t *warp_bars(unsigned char *smem, int warp, int warps_per_cta)
 {
-    return reinterpret_cast<float *>(smem) + warp * kStages * stage_floats;
-}
-__device__ __forceinline__ uint64_t *warp_bars(unsigned char *smem, int warp, int warps_per_cta,
-                                               int stage_floats = kStageFloats)
-{
-    return reinterpret_cast<uint64_t *>(smem + warps_per_cta * kStages * stage_floats * 4) + warp * kStages;
+    return reinterpret_cast<uint64_t *>(smem + warps_per_cta * kStages * kStageFloats * 4) + warp * kStages;
 }
 __device__ __forceinline__ void init_bars(uint64_t *bars, int lane)
 {
