@@ -139,20 +139,22 @@ namespace {
 
 // Segment length of a 2D level, measured on 16384^2 (level kernel times and
 // the whole forward + inverse step, CUDA events): the forward is fastest with
-// about 176 segments per level (none shorter than 8 pairs from 1024 row
-// pairs up, 2 below); the inverse with about 256 on large levels (88: inverse
-// level 0 in 0.361 ms, 176: 0.350, 256: 0.342, 384: 0.338, step best at
-// 256) and 128 (at least 2 pairs) from 1024 row pairs down.
+// about 176 segments per level (none shorter than 4 pairs from 1024 row
+// pairs up, 2 below); the inverse with about 384 on large levels, none
+// shorter than 16 pairs (88 segments: inverse level 0 in 0.361 ms, 176:
+// 0.350, 256: 0.342, 384: 0.337; the step 1.052 / 1.022 / 1.009 ms at 88 /
+// 256 / 384-and-16) and 128 (at least 2 pairs) from 1024 row pairs down.
 constexpr int kSegsForward = 176;
-constexpr int kSegsInverse = 256;
+constexpr int kSegsInverse = 384;
 constexpr int kSegsInverseSmall = 128;
 constexpr int kSmallPairs = 1024;
 // Below kSmallPairs the levels are latency-bound: segments as short as 2
 // pairs (more, shorter units) measured 5 us faster per 16384^2 forward +
 // inverse than a 4-pair minimum.
 constexpr int kSegMinSmall = 2;
-// Shortest forward segment from kSmallPairs row pairs up.
-constexpr int kSegMinForward = 8;
+// Shortest forward / inverse segment above kSmallPairs row pairs.
+constexpr int kSegMinForward = 4;
+constexpr int kSegMinInverse = 16;
 
 int env_int(const char *name, int dflt)
 {
@@ -179,10 +181,11 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
             static const int segs_i = std::max(1, env_int("DWT_GPU_SEGS_INV", kSegsInverse));
             static const int segs_is = std::max(1, env_int("DWT_GPU_SEGS_INV_SMALL", kSegsInverseSmall));
             static const int fwd_min = std::max(1, env_int("DWT_GPU_SEG_MIN_FWD", kSegMinForward));
+            static const int inv_min = std::max(1, env_int("DWT_GPU_SEG_MIN_INV", kSegMinInverse));
             if (!inverse)
                 seg = std::max(ceil_div(npairs, segs_f), npairs >= kSmallPairs ? fwd_min : kSegMinSmall);
             else if (npairs > kSmallPairs)
-                seg = std::max(ceil_div(npairs, segs_i), 4);
+                seg = std::max(ceil_div(npairs, segs_i), inv_min);
             else
                 seg = std::max(ceil_div(npairs, segs_is), kSegMinSmall);
         }
