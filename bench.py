@@ -191,11 +191,15 @@ def cpu_checks(threads: int, main_img, main_coef, main_rec, checks: dict) -> dic
         out["c0_cdf97_fwd_j5"] = rel(coef0, ref0)
     if "c2" in checks:
         worst = {"max_rel": 0.0, "rms_rel": 0.0}
-        for img2, out2, wav, jj in checks["c2"]:
+        worst_rt = {"max_rel": 0.0, "rms_rel": 0.0}
+        for img2, out2, wav, jj, back2 in checks["c2"]:
             ref2, _ = O.transform2_dense(img2, wav, "f", jj, 0, "d", threads)
             e = rel(out2, ref2)
             worst = {k: max(worst[k], e[k]) for k in worst}
+            e = rel(back2, img2.astype(np.float64))
+            worst_rt = {k: max(worst_rt[k], e[k]) for k in worst_rt}
         out["c2_sample_fwd_worst"] = dict(worst, images=len(checks["c2"]))
+        out["c2_sample_roundtrip_worst"] = dict(worst_rt, images=len(checks["c2"]))
     if "c4" in checks:
         part, gpu_part, n, st, count, lanes, gs = checks["c4"]
         ref4 = part.copy()
@@ -400,9 +404,10 @@ def main():
     err_rt = float((rec - src).abs().max().item())
 
     # level 0 alone, both directions (16384^2 <-> four bands), each timed
-    # with CUDA events over `reps` back-to-back launches; the slower one is
-    # the dominant kernel of the step (its template instance runs every level
-    # of its direction and has the larger share of the step's device time)
+    # with CUDA events over `reps` back-to-back launches.  The dominant
+    # kernel is the level-kernel instance with the larger share of the step:
+    # the instance of the slower direction (it runs every level of its
+    # direction but the coarse ones), timed here as whole transforms
     bands = torch.empty_like(src)
     ll = torch.empty((H // 2, W // 2), dtype=torch.float32, device="cuda")
     rec0 = torch.empty_like(src)
@@ -432,9 +437,23 @@ def main():
         k1.record(stream)
         torch.cuda.synchronize()
         level_ms[inverse] = k0.elapsed_time(k1) / reps
+    dir_ms = {}
+    for inverse in (False, True):
+        a, b_ = (src, coef) if not inverse else (coef, rec)
+        for _ in range(2):
+            D.transform2_dev(a, b_, "cdf97", inverse, J, 0, sptr)
+        torch.cuda.synchronize()
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(5):
+            D.transform2_dev(a, b_, "cdf97", inverse, J, 0, sptr)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        dir_ms[inverse] = k0.elapsed_time(k1) / 5
     tk1 = time.time()
     level0_rt_err = float((rec0 - src).abs().max().item())  # one level forward, then inverse
-    dom_inv = level_ms[True] >= level_ms[False]
+    dom_inv = dir_ms[True] >= dir_ms[False]
     kms = level_ms[dom_inv]
     alg_bytes = 8 * W * H
     achieved = alg_bytes / (kms / 1e3) / 1e9
@@ -500,6 +519,7 @@ def main():
                                         else "level_kernel<4,true> (CDF 9/7 inverse, level 0)"),
                              "launch_ms": round(level_ms[not dom_inv], 4),
                              "frac": round(alg_bytes / (level_ms[not dom_inv] / 1e3) / 1e9 / peak, 4)},
+                         "direction_ms": {"forward": round(dir_ms[False], 4), "inverse": round(dir_ms[True], 4)},
                          "level0_roundtrip_max_abs_err": level0_rt_err,
                          "step_bytes": step_bytes,
                          "step_frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4)},
@@ -913,16 +933,35 @@ def run_batch_extra(D, torch, stream, sptr, checks: dict, n_images=4096, j=4):
     maxdiff = 0.0
     for k in range(len(sizes)):
         maxdiff = max(maxdiff, float((work[k] - dsts[k]).abs().max().item()))
-    # 32 images of the batch for the CPU leg's FP64 check
+    # the inverse of every image in one batch of its own: the round trip of
+    # all 4096 images on the device
+    backs, inv_imgs = [], []
+    for k, (w, h, wav) in enumerate(sizes):
+        pw = (w + 3) // 4 * 4
+        cbuf = torch.empty((h, pw), dtype=torch.float32, device="cuda")
+        cbuf[:, :w] = dsts[k]
+        back = torch.empty((h, w), dtype=torch.float32, device="cuda")
+        backs.append(back)
+        inv_imgs.append(dict(src=cbuf[:, :w], dst=back, wavelet="cdf97" if wav == 0 else "cdf53", inverse=True,
+                             j_levels=j))
+    bi = D.Batch(inv_imgs, b.params)
+    bi.run(sptr)
+    torch.cuda.synchronize()
+    rt_err = max(float((backs[k] - srcs[k]).abs().max().item()) for k in range(len(sizes)))
+    bi.close()
+    # 32 images of the batch for the CPU leg's FP64 check (forward and round trip)
     sample = []
     for k in range(0, len(sizes), max(1, len(sizes) // 32))[:32]:
         w, h, wav = sizes[k]
-        sample.append((srcs[k].cpu().numpy().copy(), dsts[k].cpu().numpy(), "cdf97" if wav == 0 else "cdf53", j))
+        sample.append((srcs[k].cpu().numpy().copy(), dsts[k].cpu().numpy(), "cdf97" if wav == 0 else "cdf53", j,
+                       backs[k].cpu().numpy()))
     checks["c2"] = sample
+    del backs, inv_imgs
     res = {"c2_images": n_images, "c2_pixels": total_px, "c2_batch_mpx_s": round(total_px / batch_ms / 1e3, 1),
            "c2_batch_ms": round(batch_ms, 3), "c2_plain_dropin_mpx_s": round(total_px / plain_s / 1e6, 1),
            "c2_speedup_vs_plain": round((total_px / batch_ms / 1e3) / (total_px / plain_s / 1e6), 1),
            "c2_max_abs_diff_vs_plain": maxdiff, "c2_autotuned_params": list(b.params),
+           "c2_roundtrip_max_abs_err_all_images": rt_err,
            "c2_items": b.items, "c2_plan_s": round(plan_s, 2)}
     b.close()
     return res
