@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -1302,6 +1303,133 @@ static int run_1d_d(int wavelet, bool inverse, const double *a, const double *b,
     return set_error(check_device_error(c));
 }
 
+// ------------------------------------------- strided 1D: combined calls
+//
+// The reference's callers transform banks of signals as loops of one
+// dwt_cdf97_f_ex_stride_s call per signal, often from several OpenMP threads
+// at once (src/libdwt.c:5512-5557).  One call costs a few launches and a
+// synchronisation, tens of microseconds, almost all of it fixed cost; so
+// calls that arrive while another thread's batch is on the GPU are combined:
+// the thread that finds no batch running takes every pending call, gathers
+// their samples into the rows of one frame, transforms all rows in one
+// launch per (wavelet, direction, length) and scatters the results, and the
+// calls it took return once that has synchronised.  A thread calling alone
+// gets a batch of one.  Only calls whose memory the kernels address
+// directly are combined (device and managed memory, and pageable host memory
+// where the GPU walks the host's page tables); the others take the per-call
+// path below.  DWT_GPU_COMBINE_1D=0 turns combining off.
+struct PendingCall {
+    int wavelet;
+    bool inverse;
+    int N;
+    CallRow row;
+    int rc;
+    bool done;
+};
+
+static std::mutex g_comb_mu;
+static std::condition_variable g_comb_cv;
+static std::vector<PendingCall *> g_comb_pending;
+static bool g_comb_running = false;
+
+static bool combine_enabled()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_COMBINE_1D");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+static bool kernel_reaches(const void *p)
+{
+    const MemKind k = classify(p);
+    return k == MemKind::Device || k == MemKind::Managed || (k == MemKind::Pageable && pageable_direct());
+}
+
+// One (wavelet, direction, length) group of combined calls: gather, one
+// launch over all rows, scatter, synchronise.
+static int run_1d_rows(int wavelet, bool inverse, int N, PendingCall *const *calls, int n)
+{
+    if (n > 65535) return set_error(DWT_GPU_EINVAL);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
+    cudaStream_t s = c.stream;
+    const int nl = (N + 1) / 2;
+    const int nl4 = int(align_up(nl, 4));
+    const long long P = align_up(N + 4, 32);
+    std::vector<CallRow> rows(n);
+    for (int k = 0; k < n; ++k) rows[k] = calls[k]->row;
+    Buf desc(sizeof(CallRow) * n + 256, s), in(size_t(P) * n * 4 + 256, s), out(size_t(P) * n * 4 + 256, s);
+    if (!desc.p || !in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
+    CK(cudaMemcpyAsync(desc.p, rows.data(), sizeof(CallRow) * n, cudaMemcpyHostToDevice, s));
+    const CallRow *d_rows = static_cast<const CallRow *>(desc.p);
+    CK(launch_gather_calls(d_rows, n, N, inverse, in.f(), P, nl4, s));
+    LevelDesc d{};
+    d.w = N;
+    d.h = n;
+    d.rows_only = 1;
+    d.in[0] = in.f();
+    d.in_pitch[0] = P;
+    if (inverse) {
+        d.in[1] = in.f() + nl4;
+        d.in_pitch[1] = P;
+    }
+    d.out[0] = out.f();
+    d.out_pitch[0] = P;
+    if (!inverse) {
+        d.out[1] = out.f() + nl;
+        d.out_pitch[1] = P;
+    }
+    plan_level(d, 0, inverse);
+    CK(launch_level(d, wavelet, inverse, s, c.d_err));
+    CK(launch_scatter_calls(d_rows, n, N, inverse, out.f(), P, s));
+    CK(cudaStreamSynchronize(s));
+    return set_error(check_device_error(c));
+}
+
+static void run_combined(std::vector<PendingCall *> &batch)
+{
+    std::stable_sort(batch.begin(), batch.end(), [](const PendingCall *x, const PendingCall *y) {
+        if (x->wavelet != y->wavelet) return x->wavelet < y->wavelet;
+        if (x->inverse != y->inverse) return x->inverse < y->inverse;
+        return x->N < y->N;
+    });
+    for (size_t i = 0; i < batch.size();) {
+        size_t j = i + 1;
+        while (j < batch.size() && batch[j]->wavelet == batch[i]->wavelet && batch[j]->inverse == batch[i]->inverse &&
+               batch[j]->N == batch[i]->N)
+            ++j;
+        const int rc = run_1d_rows(batch[i]->wavelet, batch[i]->inverse, batch[i]->N, batch.data() + i, int(j - i));
+        for (size_t k = i; k < j; ++k) batch[k]->rc = rc;
+        i = j;
+    }
+}
+
+// Queues the call and returns when a batch holding it completed (running
+// that batch itself when none is running).
+static int run_1d_combined(PendingCall &me)
+{
+    std::unique_lock<std::mutex> lk(g_comb_mu);
+    g_comb_pending.push_back(&me);
+    while (!me.done) {
+        if (!g_comb_running) {
+            g_comb_running = true;
+            std::vector<PendingCall *> batch;
+            batch.swap(g_comb_pending);
+            lk.unlock();
+            run_combined(batch);
+            lk.lock();
+            for (PendingCall *q : batch) q->done = true;
+            g_comb_running = false;
+            g_comb_cv.notify_all();
+        } else {
+            g_comb_cv.wait(lk);
+        }
+    }
+    return me.rc;
+}
+
 int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l, float *h_out, int N,
            int stride)
 {
@@ -1314,6 +1442,20 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
     if (stride < 4) {
         log_error("stride %d smaller than a sample\n", stride);
         return set_error(DWT_GPU_EINVAL);
+    }
+    if (!a || !c_l || (inverse && N / 2 > 0 && !b) || (!inverse && N / 2 > 0 && !h_out)) {
+        log_error("null 1D signal pointer\n");
+        return set_error(DWT_GPU_EINVAL);
+    }
+    if (combine_enabled()) {
+        const int nh = N / 2;
+        const bool reach = kernel_reaches(a) && kernel_reaches(c_l) &&
+                           (!inverse || nh == 0 || (b && kernel_reaches(b))) &&
+                           (inverse || nh == 0 || (h_out && kernel_reaches(h_out)));
+        if (reach) {
+            PendingCall me{wavelet, inverse, N, CallRow{a, b, c_l, h_out, stride}, DWT_GPU_OK, false};
+            return set_error(run_1d_combined(me));
+        }
     }
     const NvtxRange range("dwt 1D %s %s N=%d", wavelet == CDF97 ? "cdf97" : "cdf53", inverse ? "inverse" : "forward",
                           N);

@@ -275,6 +275,43 @@ __global__ void zero_rects_kernel(float *f, long long pitch, const ZeroRects R)
     }
 }
 
+// Signals of separate calls gathered into the rows of a compact frame and
+// scattered back: call k's samples i live at a[k] + i * stride[k] bytes
+// (forward: N samples; inverse: ceil(N/2) of L at a[k] into [0, ..) and
+// floor(N/2) of H at b[k] into [h_off, ..)); results go to c[k] (forward: L
+// and then H to h[k]; inverse: N samples), same strides.
+__global__ void gather_calls_kernel(const CallRow *calls, int n_calls, int N, bool inverse, float *dst,
+                                    long long dpitch, int h_off)
+{
+    const int k = blockIdx.y;
+    if (k >= n_calls) return;
+    const CallRow r = calls[k];
+    float *row = dst + (long long)k * dpitch;
+    const int nl = (N + 1) / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        if (!inverse || i < nl)
+            row[i] = load_any(static_cast<const unsigned char *>(r.a) + (long long)i * r.stride);
+        else
+            row[h_off + (i - nl)] = load_any(static_cast<const unsigned char *>(r.b) + (long long)(i - nl) * r.stride);
+    }
+}
+
+__global__ void scatter_calls_kernel(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
+                                     long long spitch)
+{
+    const int k = blockIdx.y;
+    if (k >= n_calls) return;
+    const CallRow r = calls[k];
+    const float *row = src + (long long)k * spitch;
+    const int nl = (N + 1) / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        if (inverse || i < nl)
+            store_any(static_cast<unsigned char *>(r.c) + (long long)i * r.stride, row[i]);
+        else
+            store_any(static_cast<unsigned char *>(r.h) + (long long)(i - nl) * r.stride, row[i]);
+    }
+}
+
 // Interleaved channels (pixel = `channels` floats) <-> one compact plane per
 // channel, plane c at planes + c * plane_stride (pitch in floats).
 __global__ void deinterleave_kernel(const unsigned char *src, long long src_pitch, int channels, int w, int h,
@@ -422,6 +459,26 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
     scatter_signals_kernel<<<grid_for((long long)N * count, 256), 256, 0, s>>>(
         src, spitch, N, static_cast<unsigned char *>(base), stride, count, group, group_stride,
         lane_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_calls(const CallRow *calls, int n_calls, int N, bool inverse, float *dst, long long dpitch,
+                                int h_off, cudaStream_t s)
+{
+    if (n_calls <= 0 || N <= 0) return cudaSuccess;
+    if (n_calls > 65535) return cudaErrorInvalidValue;
+    const dim3 grid(unsigned(std::min(ceil_div(N, 256), 64)), unsigned(n_calls));
+    gather_calls_kernel<<<grid, 256, 0, s>>>(calls, n_calls, N, inverse, dst, dpitch, h_off);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_calls(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
+                                 long long spitch, cudaStream_t s)
+{
+    if (n_calls <= 0 || N <= 0) return cudaSuccess;
+    if (n_calls > 65535) return cudaErrorInvalidValue;
+    const dim3 grid(unsigned(std::min(ceil_div(N, 256), 64)), unsigned(n_calls));
+    scatter_calls_kernel<<<grid, 256, 0, s>>>(calls, n_calls, N, inverse, src, spitch);
     return cudaGetLastError();
 }
 

@@ -40,6 +40,20 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
                                    long long count, int group, long long group_stride,
                                    long long lane_stride, cudaStream_t s);
 
+// One strided 1D call of a combined batch: its sources (a; the inverse's H
+// from b), its destinations (c; the forward's H to h) and its byte stride.
+struct CallRow {
+    const void *a, *b;
+    void *c, *h;
+    long long stride;
+};
+// The calls' signals (N samples each) into the rows of a compact frame
+// (inverse: L at the row's start, H from h_off), and the rows' results back.
+cudaError_t launch_gather_calls(const CallRow *calls, int n_calls, int N, bool inverse, float *dst, long long dpitch,
+                                int h_off, cudaStream_t s);
+cudaError_t launch_scatter_calls(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
+                                 long long spitch, cudaStream_t s);
+
 // The per-line levels of a sparse frame with zero padding in one CTA, the
 // frame of level j0 held in shared memory: forward levels j0 .. j1-1 or
 // inverse levels j1 .. j0+1.  Only when sparse_tail_smem(ox, oy, j0) fits
