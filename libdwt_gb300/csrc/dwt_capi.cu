@@ -720,17 +720,20 @@ static int pipelined_inverse(Lane &c, int wavelet, char *host, long long sx, int
 // reads the top-left quadrant and the LL scratch and writes the top-left
 // quadrant, which level 0 no longer reads (forward) or does not touch until
 // they are done (inverse).  So:
-//   forward: level 0 reads the frame and writes its three detail bands to a
-//            staging frame T (LL1 to scratch); then, on a second stream, the
-//            three quadrants are copied from T into the frame while levels
-//            1 .. J-1 run on the first and write the top-left quadrant;
-//   inverse: the three detail quadrants are copied from the frame into T on
-//            a second stream while levels J .. 2 read the top-left quadrant;
-//            level 1 then reads LL1 and the details from T and writes the
-//            whole frame.
-// Extra traffic: 6 bytes per pixel (three quarters of the frame read and
-// written once) instead of 8 for a staged copy of the whole frame, and the
-// copy overlaps the coarser, latency-bound levels.
+//   forward: level 0 reads the frame and writes the detail rows it may not
+//            write in place yet to a staging frame T (LL1 to scratch); then,
+//            on a second stream, those are copied from T into the frame while
+//            levels 1 .. J-1 run on the first and write the top-left quadrant;
+//   inverse: the detail rows level 0 could overwrite before reading them are
+//            copied from the frame into T on a second stream while levels
+//            J .. 2 read the top-left quadrant; level 0 then reads LL1, the
+//            staged details from T and the others from the frame, and writes
+//            the whole frame.
+// Which rows need T follows from running level 0 in row bands in a fixed
+// order (inplace_device): the HL quadrant and the LH / HH rows of the last
+// one or two bands, about 3/8 of the frame read and written once (3 bytes per
+// pixel) instead of 8 bytes per pixel for a staged copy of the whole frame,
+// and the copies overlap the coarser, latency-bound levels.
 constexpr long long kInPlaceMinPixels = 1LL << 20;
 
 // DWT_GPU_SPARSE_FUSED=0 keeps sparse frames on the per-line sequence.
@@ -759,12 +762,44 @@ static bool inplace_device_ok(const void *ptr, long long sx_bytes, int W, int H,
            (reinterpret_cast<uintptr_t>(ptr) & 15) == 0 && coarse_level(W, H, J) >= 1;
 }
 
+// Level 0 of an in-place transform (the last level of the inverse) runs as
+// a few launches (4; DWT_GPU_INPLACE_BANDS, 3..64) over consecutive row bands, in an order that lets
+// most bands write (forward) or read (inverse) the LH and HH rows in the
+// caller's frame itself: the forward from the bottom up -- a band's LH / HH
+// rows (hs + its pairs) lie below every row a later band reads -- and the
+// inverse from the top down -- a band reads LH / HH rows no earlier band has
+// written.  The host checks each band's rows against every band that reads
+// or writes after it (row intervals with the lifting warm-up and mirrored
+// rows, plus a margin) and stages only the bands that fail (the last one or
+// two) and the HL quadrant, whose top-down and bottom-up hazards cannot be
+// ordered away.  Launches in one stream complete in order (the programmatic
+// dependent launch of each waits for its predecessor's completion before any
+// memory access).  On a 16384^2 CDF 9/7 pair 4 bands took 1.487 ms, 8 bands
+// 1.555 ms and 16 bands 1.747 ms: each band is a launch with its own ramp
+// and tail, which outweighs the smaller staged share of more bands.
+static int inplace_bands()
+{
+    static const int n = [] {
+        const char *e = getenv("DWT_GPU_INPLACE_BANDS");
+        const int v = e ? atoi(e) : 0;
+        return v >= 3 && v <= 64 ? v : 4;
+    }();
+    return n;
+}
+
+struct RowSpan {
+    long long lo, hi;  // [lo, hi)
+    bool empty() const { return hi <= lo; }
+    bool meets(const RowSpan &o) const { return !empty() && !o.empty() && lo < o.hi && o.lo < hi; }
+};
+
 static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long long sx_bytes, int W, int H, int J)
 {
     cudaStream_t s = c.stream, s2 = c.s_in;
     const long long Fp = sx_bytes / 4;
     const long long P = align_up(W, 32);
     const int ws = (W + 1) / 2, hs = (H + 1) / 2;
+    const int LAT = wavelet == CDF97 ? 2 : 1;
     Buf T(size_t(P) * H * 4 + 256, s);
     long long p0, p1;
     const size_t sf = dense_scratch_floats(W, H, J, &p0, &p1);
@@ -775,36 +810,106 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
     scratch_frames(W, H, J, scratch.f(), buf, p);
     cudaEvent_t e_start = c.event(0), e_copy = c.event(1);
     if (!e_start || !e_copy) return set_error(DWT_GPU_ECUDA);
-    // the three detail quadrants between the frame and T (same positions):
-    // the right part of the top rows, then the whole bottom rows
-    auto copy_details = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
+
+    // level 0 (forward) / the last inverse level, planned as one launch
+    LevelDesc d0 = inverse ? inv_desc(T.f(), P, F, Fp, W, H, J, 1, buf, p)
+                           : fwd_desc(F, Fp, T.f(), P, W, H, J, 0, buf, p);
+    plan_level(d0, 0, inverse);
+    const int npairs = hs, S = d0.seg_pairs, nsegs = d0.n_segs;
+    const int K = std::min(inplace_bands(), nsegs);
+    // band k in processing order: its segments and row pairs
+    auto band_segs = [&](int k, int &sg0, int &sg1) {
+        if (!inverse) {  // bottom up
+            sg0 = nsegs - int((long long)(k + 1) * nsegs / K);
+            sg1 = nsegs - int((long long)k * nsegs / K);
+        } else {  // top down
+            sg0 = int((long long)k * nsegs / K);
+            sg1 = int((long long)(k + 1) * nsegs / K);
+        }
+    };
+    std::vector<RowSpan> pairs_of(K);
+    for (int k = 0; k < K; ++k) {
+        int a, b;
+        band_segs(k, a, b);
+        pairs_of[k] = RowSpan{(long long)a * S, std::min<long long>(npairs, (long long)b * S)};
+    }
+    const long long margin = 2;
+    // forward: the image rows a band reads; its LH / HH rows
+    auto fwd_reads = [&](const RowSpan &q) {
+        return RowSpan{std::max(0LL, 2 * (q.lo - LAT) - margin), std::min<long long>(H, 2 * (q.hi + LAT) + margin)};
+    };
+    auto fwd_detail_rows = [&](const RowSpan &q) { return RowSpan{hs + q.lo, std::min<long long>(H, hs + q.hi)}; };
+    // inverse: the frame rows of LH / HH a band reads; the image rows it writes
+    auto inv_reads = [&](const RowSpan &q) {
+        return RowSpan{hs + std::max(0LL, q.lo - LAT - margin), std::min<long long>(H, hs + q.hi + LAT + margin)};
+    };
+    auto inv_writes = [&](const RowSpan &q) { return RowSpan{2 * q.lo, std::min<long long>(H, 2 * q.hi)}; };
+    std::vector<char> in_frame(K, 0);  // forward: LH/HH written to F; inverse: LH/HH read from F
+    long long staged_lo = H;           // the LH/HH rows staged through T: [staged_lo, H)
+    for (int k = 0; k < K; ++k) {
+        bool ok = true;
+        if (!inverse) {
+            const RowSpan w = fwd_detail_rows(pairs_of[k]);
+            for (int later = k; later < K && ok; ++later) ok = !w.meets(fwd_reads(pairs_of[later]));
+            if (!ok) staged_lo = std::min(staged_lo, w.lo);
+        } else {
+            const RowSpan r = inv_reads(pairs_of[k]);
+            for (int earlier = 0; earlier <= k && ok; ++earlier) ok = !inv_writes(pairs_of[earlier]).meets(r);
+            if (!ok) staged_lo = std::min(staged_lo, r.lo);
+        }
+        in_frame[k] = ok;
+    }
+    if (!inverse) {
+        // every forward band staged below staged_lo must be too (its rows are
+        // copied back as one span)
+        for (int k = 0; k < K; ++k)
+            if (fwd_detail_rows(pairs_of[k]).lo >= staged_lo) in_frame[k] = 0;
+    }
+    // the HL quadrant and the staged LH / HH rows between the frame and T
+    auto copy_staged = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
         cudaError_t e = cudaSuccess;
         if (W > ws) e = launch_copy_rows_dev(dst + ws, dp * 4, src + ws, sp * 4, (W - ws) * 4LL, hs, s2);
-        if (e == cudaSuccess && H > hs)
-            e = launch_copy_rows_dev(dst + hs * dp, dp * 4, src + hs * sp, sp * 4, W * 4LL, H - hs, s2);
+        if (e == cudaSuccess && staged_lo < H)
+            e = launch_copy_rows_dev(dst + staged_lo * dp, dp * 4, src + staged_lo * sp, sp * 4, W * 4LL,
+                                     H - staged_lo, s2);
         return e;
     };
+    auto launch_band = [&](int k) -> cudaError_t {
+        int a, b;
+        band_segs(k, a, b);
+        LevelDesc d = d0;
+        d.seg_base = a;
+        d.n_segs = b - a;
+        if (d.n_segs <= 0) return cudaSuccess;
+        if (in_frame[k]) {
+            if (!inverse) {
+                d.out[2] = F + (long long)hs * Fp;
+                d.out[3] = F + (long long)hs * Fp + ws;
+                d.out_pitch[2] = d.out_pitch[3] = Fp;
+            } else {
+                d.in[2] = F + (long long)hs * Fp;
+                d.in[3] = F + (long long)hs * Fp + ws;
+                d.in_pitch[2] = d.in_pitch[3] = Fp;
+            }
+        }
+        return launch_level(d, wavelet, inverse, s, c.d_err);
+    };
     if (!inverse) {
-        LevelDesc d = fwd_desc(F, Fp, T.f(), P, W, H, J, 0, buf, p);
-        plan_level(d, 0, false);
-        CK(launch_level(d, wavelet, false, s, c.d_err));
+        for (int k = 0; k < K; ++k) CK(launch_band(k));
         CK(cudaEventRecord(e_start, s));
         CK(cudaStreamWaitEvent(s2, e_start, 0));
-        CK(copy_details(F, Fp, T.f(), P));
+        CK(copy_staged(F, Fp, T.f(), P));
         CK(cudaEventRecord(e_copy, s2));
         CK(dense_forward_levels(F, Fp, F, Fp, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
         CK(cudaStreamWaitEvent(s, e_copy, 0));
     } else {
         CK(cudaEventRecord(e_start, s));
         CK(cudaStreamWaitEvent(s2, e_start, 0));
-        CK(copy_details(T.f(), P, F, Fp));
+        CK(copy_staged(T.f(), P, F, Fp));
         CK(cudaEventRecord(e_copy, s2));
         CK(dense_inverse_levels(F, Fp, F, Fp, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
         CK(cudaStreamWaitEvent(s, e_copy, 0));
-        LevelDesc d = inv_desc(T.f(), P, F, Fp, W, H, J, 1, buf, p);
-        plan_level(d, 0, true);
-        d.reverse = kAlternateOrder && ((coarse_level(W, H, J) - 1) & 1);
-        CK(launch_level(d, wavelet, true, s, c.d_err));
+        for (int k = 0; k < K; ++k) CK(launch_band(k));
     }
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));

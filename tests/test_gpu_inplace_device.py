@@ -1,6 +1,6 @@
 """The drop-in 2D calls (dwt_cdf{97,53}_2{f,i}_s) on dense device frames of
-1 Mpx and more, which run in place and stage only level 0's three detail
-quadrants: bit-exact against the oracle for square, odd and pitched frames,
+1 Mpx and more, which run in place with level 0 in row bands that stage only
+the HL quadrant and the rows no band order can protect: bit-exact against the oracle for square, odd and pitched frames,
 every sample of a row's padding (pitch > width) untouched, and the same on the
 full-size 16384 x 16384 image."""
 import numpy as np
@@ -70,3 +70,23 @@ def test_inplace_device_fullsize(env):
         D.transform2(dev, wav, "i", W * 4, 4, (W, H), (W, H), j)
         ref_i, _ = O.transform2_dense(ref_f, wav, "i", j, 0, "s", threads)
         assert np.array_equal(dev.cpu().numpy(), ref_i), f"{wav} inverse differs"
+
+
+def test_inplace_device_band_counts():
+    """The same frames with 3, 8 and 16 row bands for the in-place level 0
+    (DWT_GPU_INPLACE_BANDS, read once per process: child processes)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "import numpy as np, torch, libdwt_gb300 as D\n"
+            "from libdwt_gb300 import synth\n"
+            "import test_gpu_inplace_device as T\n"
+            "env = (D, torch, synth)\n"
+            "for c in T.CASES[:5]: T.test_inplace_device_matches_oracle(env, *c)\n"
+            "print('bands ok')\n") % (root, os.path.join(root, "tests"))
+    for bands in ("3", "8", "16"):
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=900,
+                           env=dict(os.environ, DWT_GPU_INPLACE_BANDS=bands))
+        assert r.returncode == 0 and "bands ok" in r.stdout, r.stdout + r.stderr
