@@ -321,7 +321,7 @@ def main():
     ap.add_argument("--image", type=int, default=16384,
                     help="image side (a smaller case for profiler captures)")
     ap.add_argument("--dropin-reps", type=int, default=10, help="timed pairs of each drop-in extra")
-    ap.add_argument("--only", choices=["c2", "c3", "c4", "dropin", "sparse"], default=None,
+    ap.add_argument("--only", choices=["c2", "c3", "c4", "dropin", "dropin-dense", "sparse"], default=None,
                     help="run one secondary configuration alone and print its figures "
                          "(for profiler captures)")
     ap.add_argument("--c4-groups", type=int, default=8192, help="signal groups of C4 (8 signals each)")
@@ -353,6 +353,9 @@ def main():
             res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks)
         elif args.only == "dropin":
             res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda(), args.dropin_reps)
+        elif args.only == "dropin-dense":
+            res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda(), args.dropin_reps,
+                                   parts=("dense",))
         elif args.only == "sparse":
             res = run_dropin_extra(D, torch, None, args.dropin_reps, parts=("sparse",))
         else:

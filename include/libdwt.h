@@ -448,6 +448,28 @@ DWT_EXPORT int dwt_gpu_dense_launches(int w, int h, int j_levels);
  * code), and the context stays usable.  DWT_GPU_EINVAL for iterations <= 0. */
 DWT_EXPORT int dwt_gpu_selftest_wait_timeout(int iterations);
 
+/* No counterpart in the reference.  Test hook of the ordered in-place level
+ * (the drop-in 2D calls on device frames): one warp waits, through the same
+ * bounded wait, for segments of a level that nothing finishes, limited to
+ * `iterations` polls; the wait gives up, sets the device error word and
+ * returns.  The call reports DWT_GPU_EDEVICE (and logs the code); the context
+ * stays usable.  DWT_GPU_EINVAL for iterations <= 0. */
+DWT_EXPORT int dwt_gpu_selftest_inplace_wait_timeout(int iterations);
+
+/* No counterpart in the reference.  The plan of level 0 of an in-place
+ * transform of a w x h image in a device frame whose LH / HH bands start at
+ * frame row detail_row ((h + 1) / 2 when negative: a dense frame; the outer
+ * midpoint of a zero-padded sparse frame), host only, no device work:
+ * segments of *seg_pairs row pairs, *n_segs of them, handed out bottom-up
+ * (forward) or top-down (inverse); segments >= *stage_seg pass their LH / HH
+ * rows through the staging frame.  When `readers` is not null it receives,
+ * per segment s, the inclusive range readers[2s] .. readers[2s+1] of the
+ * segments that must finish before s writes into the frame (empty when the
+ * second is smaller).  For tests and tuning; DWT_GPU_EINVAL for w or h < 2
+ * or 0 <= detail_row < (h + 1) / 2. */
+DWT_EXPORT int dwt_gpu_inplace_plan(int wavelet, int inverse, int w, int h, int detail_row, int *seg_pairs,
+                                    int *n_segs, int *stage_seg, int *readers);
+
 /* Waits for all device work and reports (and clears) a device-side error:
  * DWT_GPU_EDEVICE when a bounded device-side wait of the library's own
  * context or of dwt_gpu_2_dev_noalloc (on any device it ran on) gave up.

@@ -42,18 +42,6 @@ namespace dwt {
 
 namespace {
 
-__device__ __forceinline__ int ld_acquire(const int *p)
-{
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void fence_proxy_async_global()
-{
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-}
-
 // The level descriptor of forward level j (LL_j -> LL_{j+1} + details) or of
 // inverse level j (LL_j + details -> LL_{j-1}) of image I.
 __device__ LevelDesc level_desc(const BatchImage &I, int j)

@@ -301,7 +301,7 @@ constexpr bool kAlternateOrder = true;
 // Forward levels j_begin .. J-1 (the coarse kernel takes over once the band fits).
 static cudaError_t dense_forward_levels(const float *in, long long in_pitch, float *out, long long out_pitch,
                                         int W, int H, int J, int j_begin, int wavelet, float *scratch,
-                                        cudaStream_t s, int *err, int seg_hint)
+                                        cudaStream_t s, int *err, int seg_hint, cudaEvent_t after_first = nullptr)
 {
     float *buf[2];
     long long p[2];
@@ -313,6 +313,7 @@ static cudaError_t dense_forward_levels(const float *in, long long in_pitch, flo
         plan_level(d, seg_hint, false);
         d.reverse = kAlternateOrder && ((j - j_begin) & 1);
         cudaError_t e = launch_level(d, wavelet, false, s, err);
+        if (e == cudaSuccess && after_first && j == j_begin) e = cudaEventRecord(after_first, s);
         if (e != cudaSuccess) return e;
     }
     if (j0 < J) {
@@ -762,36 +763,51 @@ static bool inplace_device_ok(const void *ptr, long long sx_bytes, int W, int H,
            (reinterpret_cast<uintptr_t>(ptr) & 15) == 0 && coarse_level(W, H, J) >= 1;
 }
 
-// Level 0 of an in-place transform (the last level of the inverse) runs as
-// a few launches (4; DWT_GPU_INPLACE_BANDS, 3..64) over consecutive row bands, in an order that lets
-// most bands write (forward) or read (inverse) the LH and HH rows in the
-// caller's frame itself: the forward from the bottom up -- a band's LH / HH
-// rows (hs + its pairs) lie below every row a later band reads -- and the
-// inverse from the top down -- a band reads LH / HH rows no earlier band has
-// written.  The host checks each band's rows against every band that reads
-// or writes after it (row intervals with the lifting warm-up and mirrored
-// rows, plus a margin) and stages only the bands that fail (the last one or
-// two) and the HL quadrant, whose top-down and bottom-up hazards cannot be
-// ordered away.  Launches in one stream complete in order (the programmatic
-// dependent launch of each waits for its predecessor's completion before any
-// memory access).  On a 16384^2 CDF 9/7 pair 4 bands took 1.487 ms, 8 bands
-// 1.555 ms and 16 bands 1.747 ms: each band is a launch with its own ramp
-// and tail, which outweighs the smaller staged share of more bands.
-static int inplace_bands()
+// Level 0 of an in-place transform (the last level of the inverse) is one
+// ordered launch: its units take tickets in segment order -- bottom-up in the
+// forward, where a segment's LH / HH rows (hs + its pairs) lie below the rows
+// it and every later segment reads; top-down in the inverse, where a segment
+// reads LH / HH rows no earlier segment has written -- and each waits before
+// it starts for the earlier segments that read the rows it overwrites
+// (inplace_readers).  The segments at the end of the order, where that
+// does not hold, are staged through T, and so is the HL quadrant, whose
+// readers and writers run in the opposite order in both directions.  `lead`
+// segments more are staged so that a unit seldom waits for one still running
+// (DWT_GPU_INPLACE_LEAD, default kInPlaceLead).
+constexpr int kInPlaceLead = 16;
+
+static int inplace_lead()
 {
     static const int n = [] {
-        const char *e = getenv("DWT_GPU_INPLACE_BANDS");
-        const int v = e ? atoi(e) : 0;
-        return v >= 3 && v <= 64 ? v : 4;
+        const char *e = getenv("DWT_GPU_INPLACE_LEAD");
+        const int v = e ? atoi(e) : -1;
+        return v >= 0 && v <= 4096 ? v : kInPlaceLead;
     }();
     return n;
 }
 
-struct RowSpan {
-    long long lo, hi;  // [lo, hi)
-    bool empty() const { return hi <= lo; }
-    bool meets(const RowSpan &o) const { return !empty() && !o.empty() && lo < o.hi && o.lo < hi; }
-};
+// First staged segment of an ordered in-place level (segments >= it go
+// through T): forward, the first segment (top-down) whose readers do not all
+// come at least lead + 1 segments earlier in the bottom-up order; inverse,
+// the largest bound that leaves every writer's in-frame readers at least
+// lead + 1 segments earlier in the top-down order.
+static int inplace_stage_seg(int h, int S, int nsegs, int lat, bool inverse, int lead, int dy)
+{
+    int a, b;
+    if (!inverse) {
+        for (int s = 0; s < nsegs; ++s) {
+            inplace_readers(h, S, nsegs, lat, false, s, nsegs, dy, a, b);
+            if (b >= a && a <= s + lead) return s;
+        }
+        return nsegs;
+    }
+    int st = nsegs;
+    for (int w = 0; w < nsegs; ++w) {
+        inplace_readers(h, S, nsegs, lat, true, w, nsegs, dy, a, b);
+        if (b >= a && b > w - 1 - lead) st = std::min(st, w - lead);
+    }
+    return std::max(st, 0);
+}
 
 static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long long sx_bytes, int W, int H, int J)
 {
@@ -811,59 +827,38 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
     cudaEvent_t e_start = c.event(0), e_copy = c.event(1);
     if (!e_start || !e_copy) return set_error(DWT_GPU_ECUDA);
 
-    // level 0 (forward) / the last inverse level, planned as one launch
+    // level 0 (forward) / the last inverse level: HL in T, LH / HH in the
+    // frame except for the staged segments
     LevelDesc d0 = inverse ? inv_desc(T.f(), P, F, Fp, W, H, J, 1, buf, p)
                            : fwd_desc(F, Fp, T.f(), P, W, H, J, 0, buf, p);
     plan_level(d0, 0, inverse);
-    const int npairs = hs, S = d0.seg_pairs, nsegs = d0.n_segs;
-    const int K = std::min(inplace_bands(), nsegs);
-    // band k in processing order: its segments and row pairs
-    auto band_segs = [&](int k, int &sg0, int &sg1) {
-        if (!inverse) {  // bottom up
-            sg0 = nsegs - int((long long)(k + 1) * nsegs / K);
-            sg1 = nsegs - int((long long)k * nsegs / K);
-        } else {  // top down
-            sg0 = int((long long)k * nsegs / K);
-            sg1 = int((long long)(k + 1) * nsegs / K);
-        }
-    };
-    std::vector<RowSpan> pairs_of(K);
-    for (int k = 0; k < K; ++k) {
-        int a, b;
-        band_segs(k, a, b);
-        pairs_of[k] = RowSpan{(long long)a * S, std::min<long long>(npairs, (long long)b * S)};
-    }
-    const long long margin = 2;
-    // forward: the image rows a band reads; its LH / HH rows
-    auto fwd_reads = [&](const RowSpan &q) {
-        return RowSpan{std::max(0LL, 2 * (q.lo - LAT) - margin), std::min<long long>(H, 2 * (q.hi + LAT) + margin)};
-    };
-    auto fwd_detail_rows = [&](const RowSpan &q) { return RowSpan{hs + q.lo, std::min<long long>(H, hs + q.hi)}; };
-    // inverse: the frame rows of LH / HH a band reads; the image rows it writes
-    auto inv_reads = [&](const RowSpan &q) {
-        return RowSpan{hs + std::max(0LL, q.lo - LAT - margin), std::min<long long>(H, hs + q.hi + LAT + margin)};
-    };
-    auto inv_writes = [&](const RowSpan &q) { return RowSpan{2 * q.lo, std::min<long long>(H, 2 * q.hi)}; };
-    std::vector<char> in_frame(K, 0);  // forward: LH/HH written to F; inverse: LH/HH read from F
-    long long staged_lo = H;           // the LH/HH rows staged through T: [staged_lo, H)
-    for (int k = 0; k < K; ++k) {
-        bool ok = true;
-        if (!inverse) {
-            const RowSpan w = fwd_detail_rows(pairs_of[k]);
-            for (int later = k; later < K && ok; ++later) ok = !w.meets(fwd_reads(pairs_of[later]));
-            if (!ok) staged_lo = std::min(staged_lo, w.lo);
-        } else {
-            const RowSpan r = inv_reads(pairs_of[k]);
-            for (int earlier = 0; earlier <= k && ok; ++earlier) ok = !inv_writes(pairs_of[earlier]).meets(r);
-            if (!ok) staged_lo = std::min(staged_lo, r.lo);
-        }
-        in_frame[k] = ok;
-    }
+    const int S = d0.seg_pairs, nsegs = d0.n_segs;
+    Buf order(size_t(nsegs + 1) * 4, s);
+    if (!order.p) return set_error(DWT_GPU_ENOMEM);
+    d0.order = static_cast<int *>(order.p);
+    d0.seg_base = 0;
+    d0.reverse = inverse ? 0 : 1;
+    d0.order_dy = hs;
+    d0.stage_seg = inplace_stage_seg(H, S, nsegs, LAT, inverse, inplace_lead(), hs);
+    d0.alt[0] = T.f() + (long long)hs * P;
+    d0.alt[1] = T.f() + (long long)hs * P + ws;
+    d0.alt_pitch = P;
+    float *const lh = F + (long long)hs * Fp, *const hh = F + (long long)hs * Fp + ws;
     if (!inverse) {
-        // every forward band staged below staged_lo must be too (its rows are
-        // copied back as one span)
-        for (int k = 0; k < K; ++k)
-            if (fwd_detail_rows(pairs_of[k]).lo >= staged_lo) in_frame[k] = 0;
+        d0.out[2] = lh;
+        d0.out[3] = hh;
+        d0.out_pitch[2] = d0.out_pitch[3] = Fp;
+    } else {
+        d0.in[2] = lh;
+        d0.in[3] = hh;
+        d0.in_pitch[2] = d0.in_pitch[3] = Fp;
+    }
+    // LH / HH rows that pass through T: [staged_lo, H)
+    long long staged_lo = H;
+    if (d0.stage_seg < nsegs) {
+        const long long k = (long long)d0.stage_seg * S;
+        staged_lo = inverse ? hs + std::max(0LL, k - LAT - 3) : hs + k;
+        staged_lo = std::min<long long>(H, std::max<long long>(hs, staged_lo));
     }
     // the HL quadrant and the staged LH / HH rows between the frame and T
     auto copy_staged = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
@@ -871,36 +866,21 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
         if (W > ws) e = launch_copy_rows_dev(dst + ws, dp * 4, src + ws, sp * 4, (W - ws) * 4LL, hs, s2);
         if (e == cudaSuccess && staged_lo < H)
             e = launch_copy_rows_dev(dst + staged_lo * dp, dp * 4, src + staged_lo * sp, sp * 4, W * 4LL,
-                                     H - staged_lo, s2);
+                                      H - staged_lo, s2);
         return e;
     };
-    auto launch_band = [&](int k) -> cudaError_t {
-        int a, b;
-        band_segs(k, a, b);
-        LevelDesc d = d0;
-        d.seg_base = a;
-        d.n_segs = b - a;
-        if (d.n_segs <= 0) return cudaSuccess;
-        if (in_frame[k]) {
-            if (!inverse) {
-                d.out[2] = F + (long long)hs * Fp;
-                d.out[3] = F + (long long)hs * Fp + ws;
-                d.out_pitch[2] = d.out_pitch[3] = Fp;
-            } else {
-                d.in[2] = F + (long long)hs * Fp;
-                d.in[3] = F + (long long)hs * Fp + ws;
-                d.in_pitch[2] = d.in_pitch[3] = Fp;
-            }
-        }
-        return launch_level(d, wavelet, inverse, s, c.d_err);
-    };
+    CK(cudaMemsetAsync(order.p, 0, size_t(nsegs + 1) * 4, s));
     if (!inverse) {
-        for (int k = 0; k < K; ++k) CK(launch_band(k));
-        CK(cudaEventRecord(e_start, s));
+        // the copy back starts after level 1 (HBM-bound like the copy) and
+        // runs beside the latency-bound smaller levels
+        CK(launch_level(d0, wavelet, false, s, c.d_err));
+        const bool levels = coarse_level(W, H, J) > 1;
+        if (!levels) CK(cudaEventRecord(e_start, s));
+        CK(dense_forward_levels(F, Fp, F, Fp, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0,
+                                levels ? e_start : nullptr));
         CK(cudaStreamWaitEvent(s2, e_start, 0));
         CK(copy_staged(F, Fp, T.f(), P));
         CK(cudaEventRecord(e_copy, s2));
-        CK(dense_forward_levels(F, Fp, F, Fp, W, H, J, 1, wavelet, scratch.f(), s, c.d_err, 0));
         CK(cudaStreamWaitEvent(s, e_copy, 0));
     } else {
         CK(cudaEventRecord(e_start, s));
@@ -909,7 +889,7 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
         CK(cudaEventRecord(e_copy, s2));
         CK(dense_inverse_levels(F, Fp, F, Fp, W, H, J, 2, wavelet, scratch.f(), s, c.d_err, 0));
         CK(cudaStreamWaitEvent(s, e_copy, 0));
-        for (int k = 0; k < K; ++k) CK(launch_band(k));
+        CK(launch_level(d0, wavelet, true, s, c.d_err));
     }
     CK(cudaStreamSynchronize(s));
     return set_error(check_device_error(c));
@@ -938,6 +918,49 @@ static bool sparse_fast_ok(const void *F, long long Fp, int ox, int oy, int ix, 
            ox >= ix && oy >= iy;
 }
 
+// Rectangles [x0, x1) x [y0, y1) of zero fill.
+struct ZRect {
+    int x0, y0, x1, y1;
+    bool empty() const { return x1 <= x0 || y1 <= y0; }
+};
+
+static ZRect zrect_and(const ZRect &a, const ZRect &b)
+{
+    return ZRect{std::max(a.x0, b.x0), std::max(a.y0, b.y0), std::min(a.x1, b.x1), std::min(a.y1, b.y1)};
+}
+
+// The parts of every rectangle of `in` outside k (up to four pieces each).
+static std::vector<ZRect> zrect_minus(const std::vector<ZRect> &in, const ZRect &k)
+{
+    std::vector<ZRect> out;
+    for (const ZRect &a : in) {
+        const ZRect c = zrect_and(a, k);
+        if (a.empty()) continue;
+        if (c.empty()) {
+            out.push_back(a);
+            continue;
+        }
+        const ZRect pieces[4] = {{a.x0, a.y0, a.x1, c.y0},     // above
+                                 {a.x0, c.y1, a.x1, a.y1},     // below
+                                 {a.x0, c.y0, c.x0, c.y1},     // left
+                                 {c.x1, c.y0, a.x1, c.y1}};    // right
+        for (const ZRect &p : pieces)
+            if (!p.empty()) out.push_back(p);
+    }
+    return out;
+}
+
+static void zrects_add(ZeroRects &Z, const ZRect &r)
+{
+    if (r.empty() || Z.n >= kMaxZeroRects) return;
+    Z.x0[Z.n] = r.x0;
+    Z.y0[Z.n] = r.y0;
+    Z.w[Z.n] = r.x1 - r.x0;
+    Z.first_row[Z.n] = Z.total_rows;
+    Z.total_rows += r.y1 - r.y0;
+    Z.n++;
+}
+
 static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long long Fp, int ox, int oy, int ix,
                           int iy, int J)
 {
@@ -957,18 +980,57 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
     scratch_frames(ix, iy, Js, scratch.f(), buf, p);
     cudaEvent_t e_start = c.event(0), e_copy = c.event(1);
     if (!e_start || !e_copy) return set_error(DWT_GPU_ECUDA);
-    // level 0's three detail bands between the frame and T (same positions)
+    // Level 0 (the last inverse level) is an ordered in-place launch as for
+    // dense frames, with the LH / HH bands at the outer midpoint row ody:
+    // HL and the LH / HH rows of the staged segments pass through T (same
+    // positions).
     const int odx = cdp(ox, 1), ody = cdp(oy, 1);
     const int lx = (ix + 1) / 2, hx = ix / 2, ly = (iy + 1) / 2, hy = iy / 2;
+    const int LAT = wavelet == CDF97 ? 2 : 1;
+    Buf order;
+    ZeroRects late_zeros{};
+    long long staged_lo = (long long)ody + hy;  // LH / HH rows [staged_lo, ody + hy) pass through T
+    auto order_level0 = [&](LevelDesc &d, bool inv, int dx, int dy, float *Tb, long long tp, float *Fb,
+                            long long fp) -> cudaError_t {
+        const int S = d.seg_pairs, nsegs = d.n_segs;
+        if (!order.p && !order.alloc(size_t(nsegs + 1) * 4, s)) return cudaErrorMemoryAllocation;
+        d.order = static_cast<int *>(order.p);
+        d.seg_base = 0;
+        d.reverse = inv ? 0 : 1;
+        d.order_dy = dy;
+        d.stage_seg = inplace_stage_seg(d.h, S, nsegs, LAT, inv, inplace_lead(), dy);
+        d.alt[0] = Tb + (long long)dy * tp;
+        d.alt[1] = Tb + (long long)dy * tp + dx;
+        d.alt_pitch = tp;
+        float *lh = Fb + (long long)dy * fp, *hh = Fb + (long long)dy * fp + dx;
+        if (!inv) {
+            d.out[2] = lh;
+            d.out[3] = hh;
+            d.out_pitch[2] = d.out_pitch[3] = fp;
+        } else {
+            d.in[2] = lh;
+            d.in[3] = hh;
+            d.in_pitch[2] = d.in_pitch[3] = fp;
+        }
+        if (d.stage_seg < nsegs) {
+            const long long k = (long long)d.stage_seg * S;
+            staged_lo = inv ? dy + std::max(0LL, k - LAT - 3) : dy + k;
+            staged_lo = std::min<long long>((long long)dy + hy, std::max<long long>(dy, staged_lo));
+        } else {
+            staged_lo = (long long)dy + hy;
+        }
+        return cudaMemsetAsync(order.p, 0, size_t(nsegs + 1) * 4, s);
+    };
     auto copy_details = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
         cudaError_t e = cudaSuccess;
-        auto rect = [&](int x0, int y0, int w, int h) {
+        auto rect = [&](int x0, long long y0, int w, long long h) {
             if (e == cudaSuccess && w > 0 && h > 0)
                 e = launch_copy_rows_dev(dst + y0 * dp + x0, dp * 4, src + y0 * sp + x0, sp * 4, w * 4LL, h, s2);
         };
-        rect(odx, 0, hx, ly);   // HL
-        rect(0, ody, lx, hy);   // LH
-        rect(odx, ody, hx, hy); // HH
+        const long long rows = (long long)ody + hy - staged_lo;
+        rect(odx, 0, hx, ly);             // HL
+        rect(0, staged_lo, lx, rows);     // LH of the staged segments
+        rect(odx, staged_lo, hx, rows);   // HH of the staged segments
         return e;
     };
     // tmp of the per-line levels: lines x length of the largest such frame
@@ -996,12 +1058,15 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
             d.out_pitch[1] = d.out_pitch[2] = d.out_pitch[3] = bp;
             plan_level(d, 0, false);
             d.reverse = kAlternateOrder && (j & 1);
+            if (j == 0) {
+                // ordered level 0: LH / HH into the frame but for the staged segments
+                CK(order_level0(d, false, dx, dy, T.f(), P, F, Fp));
+            }
             CK(launch_level(d, wavelet, false, s, c.d_err));
             if (j == 0) {
                 CK(cudaEventRecord(e_start, s));
                 CK(cudaStreamWaitEvent(s2, e_start, 0));
                 CK(copy_details(F, Fp, T.f(), P));
-                CK(cudaEventRecord(e_copy, s2));
                 if (jf == 1)  // LL1 into the frame for the per-line levels
                     CK(launch_copy_rows_dev(F, Fp * 4, buf[0], p[0] * 4, lx * 4LL, ly, s));
             }
@@ -1013,34 +1078,39 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
                 CK(sparse_forward_level(F, Fp, cdp(ox, j), cdp(oy, j), cdp(ox, j + 1), cdp(oy, j + 1), cdp(ix, j),
                                         cdp(iy, j), 1, wavelet, tmp.f(), s));
         }
-        CK(cudaStreamWaitEvent(s, e_copy, 0));
         // zeros where no band of the fused levels lands (the per-line levels
         // zero their own frames): per fused level, the parts of its frame
-        // outside its four bands and outside the next level's frame
-        ZeroRects R{};
-        auto add = [&](int x0, int y0, int w, int h) {
-            if (w <= 0 || h <= 0 || R.n >= kMaxZeroRects) return;
-            R.x0[R.n] = x0;
-            R.y0[R.n] = y0;
-            R.w[R.n] = w;
-            R.first_row[R.n] = R.total_rows;
-            R.total_rows += h;
-            R.n++;
+        // outside its four bands and outside the next level's frame.  Level
+        // 0's parts lie outside the frame of every later level: they are
+        // written on the second stream after level 0, beside the smaller levels
+        ZeroRects R0{}, R{};
+        auto add = [&](ZeroRects &Z, int x0, int y0, int w, int h) {
+            if (w <= 0 || h <= 0 || Z.n >= kMaxZeroRects) return;
+            Z.x0[Z.n] = x0;
+            Z.y0[Z.n] = y0;
+            Z.w[Z.n] = w;
+            Z.first_row[Z.n] = Z.total_rows;
+            Z.total_rows += h;
+            Z.n++;
         };
         for (int j = 0; j < jf; ++j) {
+            ZeroRects &Z = j == 0 ? R0 : R;
             const int ow = cdp(ox, j), oh = cdp(oy, j), dx = cdp(ox, j + 1), dy = cdp(oy, j + 1);
             const int iw = cdp(ix, j), ih = cdp(iy, j);
             const int lxj = (iw + 1) / 2, hxj = iw / 2, lyj = (ih + 1) / 2, hyj = ih / 2;
-            add(lxj, dy, dx - lxj, oh - dy);             // between the L and H columns, below the next frame
-            add(dx + hxj, 0, ow - dx - hxj, oh);         // right of the H columns
-            add(dx, lyj, hxj, dy - lyj);                 // H columns, between the L and H rows
-            add(0, dy + hyj, lxj, oh - dy - hyj);        // L columns, below the H rows
-            add(dx, dy + hyj, hxj, oh - dy - hyj);       // H columns, below the H rows
-            if (j == J - 1) {                            // the last level's frame around LL_J
-                add(lxj, 0, dx - lxj, dy);
-                add(0, lyj, lxj, dy - lyj);
+            add(Z, lxj, dy, dx - lxj, oh - dy);         // between the L and H columns, below the next frame
+            add(Z, dx + hxj, 0, ow - dx - hxj, oh);     // right of the H columns
+            add(Z, dx, lyj, hxj, dy - lyj);             // H columns, between the L and H rows
+            add(Z, 0, dy + hyj, lxj, oh - dy - hyj);    // L columns, below the H rows
+            add(Z, dx, dy + hyj, hxj, oh - dy - hyj);   // H columns, below the H rows
+            if (j == J - 1) {                           // the last level's frame around LL_J
+                add(R, lxj, 0, dx - lxj, dy);
+                add(R, 0, lyj, lxj, dy - lyj);
             }
         }
+        CK(launch_zero_rects(F, Fp, R0, s2));
+        CK(cudaEventRecord(e_copy, s2));
+        CK(cudaStreamWaitEvent(s, e_copy, 0));
         CK(launch_zero_rects(F, Fp, R, s));
     } else {
         // inverse level j rebuilds LL_{j-1} (cdp(i, j-1)) from LL_j and the
@@ -1050,9 +1120,35 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
         while (jf < J && sparse_fast_level(cdp(ix, jf), cdp(iy, jf))) ++jf;
         Buf tmp(jf < J ? line_tmp(jf) * 4 + 256 : 256, s);
         if (!tmp.p) return set_error(DWT_GPU_ENOMEM);
+        {
+            // the last level, planned first: the staged rows it reads from T
+            LevelDesc d{};
+            d.w = ix;
+            d.h = iy;
+            plan_level(d, 0, true);
+            CK(order_level0(d, true, odx, ody, T.f(), P, F, Fp));
+        }
+        ZeroRects early_zeros{};
+        {
+            const ZRect outside[2] = {{ix, 0, ox, oy}, {0, iy, ix, oy}};
+            const ZRect kept[4] = {{0, 0, odx, ody},                     // the coarser levels' quadrant
+                                   {odx, 0, odx + hx, ly},               // HL of level 0
+                                   {0, ody, lx, ody + hy},               // LH
+                                   {odx, ody, odx + hx, ody + hy}};      // HH
+            std::vector<ZRect> early(outside, outside + 2);
+            for (const ZRect &k : kept) early = zrect_minus(early, k);
+            if (early.size() <= size_t(kMaxZeroRects) / 2) {
+                for (const ZRect &e : early) zrects_add(early_zeros, e);
+                for (const ZRect &o : outside)
+                    for (const ZRect &k : kept) zrects_add(late_zeros, zrect_and(o, k));
+            } else {  // (not met by the band layout) everything after level 0
+                for (const ZRect &o : outside) zrects_add(late_zeros, o);
+            }
+        }
         CK(cudaEventRecord(e_start, s));
         CK(cudaStreamWaitEvent(s2, e_start, 0));
         CK(copy_details(T.f(), P, F, Fp));
+        CK(launch_zero_rects(F, Fp, early_zeros, s2));
         CK(cudaEventRecord(e_copy, s2));
         if (jf < J && sparse_tail_smem(ox, oy, jf) <= kSparseTailSmem) {
             CK(launch_sparse_tail(true, F, Fp, ox, oy, ix, iy, jf, J, wavelet, s));
@@ -1067,6 +1163,12 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
             d.h = cdp(iy, j - 1);
             d.in[0] = j == jf ? F : buf[(j - 1) % 2];
             d.in_pitch[0] = j == jf ? Fp : p[(j - 1) % 2];
+            if (j == 1 && jf == 1) {
+                // level 0 writes the frame rows LL_1 sits in: read LL_1 from scratch
+                CK(launch_copy_rows_dev(buf[0], p[0] * 4, F, Fp * 4, cdp(ix, 1) * 4LL, cdp(iy, 1), s));
+                d.in[0] = buf[0];
+                d.in_pitch[0] = p[0];
+            }
             const float *base = j == 1 ? T.f() : F;
             const long long bp = j == 1 ? P : Fp;
             const int sx = cdp(ox, j), sy = cdp(oy, j);
@@ -1078,20 +1180,17 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
             d.out_pitch[0] = j == 1 ? Fp : p[(j - 2) % 2];
             plan_level(d, 0, true);
             d.reverse = kAlternateOrder && ((jf - j) & 1);
-            if (j == 1) CK(cudaStreamWaitEvent(s, e_copy, 0));
+            if (j == 1) {
+                CK(order_level0(d, true, sx, sy, T.f(), P, F, Fp));
+                CK(cudaStreamWaitEvent(s, e_copy, 0));
+            }
             CK(launch_level(d, wavelet, true, s, c.d_err));
         }
-        // zero padding of the last level: everything outside the inner image
-        ZeroRects R{};
-        if (ox > ix) {
-            R.x0[R.n] = ix, R.y0[R.n] = 0, R.w[R.n] = ox - ix, R.first_row[R.n] = R.total_rows;
-            R.total_rows += oy, R.n++;
-        }
-        if (oy > iy) {
-            R.x0[R.n] = 0, R.y0[R.n] = iy, R.w[R.n] = ix, R.first_row[R.n] = R.total_rows;
-            R.total_rows += oy - iy, R.n++;
-        }
-        CK(launch_zero_rects(F, Fp, R, s));
+        // zero padding of the last level, everything outside the inner image:
+        // the parts inside the level-0 detail bands or the top-left quadrant
+        // (read by the inverse levels) after level 0, the rest -- read by
+        // nothing -- written on the second stream up front (below)
+        CK(launch_zero_rects(F, Fp, late_zeros, s));
     }
     return DWT_GPU_OK;
 }
@@ -1988,6 +2087,44 @@ int dwt_gpu_selftest_wait_timeout(int iterations)
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c.stream));
     return set_error(check_device_error(c));
+}
+
+int dwt_gpu_selftest_inplace_wait_timeout(int iterations)
+{
+    t_last_error = DWT_GPU_OK;
+    if (iterations <= 0) return set_error(DWT_GPU_EINVAL);
+    LaneGuard lane_guard(ctx());
+    Lane &c = lane_guard.get();
+    const size_t bytes = size_t(order_wait_timeout_words()) * 4;
+    Buf order(bytes, c.stream);
+    if (!order.p) return set_error(DWT_GPU_ENOMEM);
+    CK(cudaMemsetAsync(order.p, 0, bytes, c.stream));
+    CK(launch_order_wait_timeout(uint32_t(iterations), static_cast<int *>(order.p), c.d_err, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return set_error(check_device_error(c));
+}
+
+int dwt_gpu_inplace_plan(int wavelet, int inverse, int w, int h, int detail_row, int *seg_pairs, int *n_segs,
+                         int *stage_seg, int *readers)
+{
+    t_last_error = DWT_GPU_OK;
+    if ((wavelet != CDF97 && wavelet != CDF53) || w < 2 || h < 2 || !seg_pairs || !n_segs || !stage_seg ||
+        (detail_row >= 0 && detail_row < (h + 1) / 2))
+        return set_error(DWT_GPU_EINVAL);
+    LevelDesc d{};
+    d.w = w;
+    d.h = h;
+    plan_level(d, 0, inverse != 0);
+    const int lat = wavelet == CDF97 ? 2 : 1;
+    *seg_pairs = d.seg_pairs;
+    *n_segs = d.n_segs;
+    const int dy = detail_row < 0 ? (h + 1) / 2 : detail_row;
+    *stage_seg = inplace_stage_seg(h, d.seg_pairs, d.n_segs, lat, inverse != 0, inplace_lead(), dy);
+    if (readers)
+        for (int s = 0; s < d.n_segs; ++s)
+            inplace_readers(h, d.seg_pairs, d.n_segs, lat, inverse != 0, s, *stage_seg, dy, readers[2 * s],
+                            readers[2 * s + 1]);
+    return DWT_GPU_OK;
 }
 
 int dwt_gpu_sync_check(void)

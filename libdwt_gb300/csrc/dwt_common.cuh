@@ -229,11 +229,26 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
+// Acquire load of a counter another warp releases (atomicAdd after a
+// __threadfence), and the fence that orders the generic-proxy accesses seen
+// so far before this thread's later TMA (async-proxy) accesses.
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // Error codes raised by device code into the error word.
 enum DeviceError : int {
     kErrNone = 0,
     kErrWaitTimeout = 1,   // an mbarrier wait gave up
-    kErrQueueTimeout = 2,  // a work-queue dependency wait gave up
+    kErrQueueTimeout = 2,  // a work-queue dependency wait gave up (batch phases, ordered in-place units)
 };
 
 // Programmatic dependent launch.  A kernel launched by launch_pdl may be

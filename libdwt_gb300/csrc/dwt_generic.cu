@@ -271,7 +271,13 @@ __global__ void zero_rects_kernel(float *f, long long pitch, const ZeroRects R)
         while (k + 1 < R.n && R.first_row[k + 1] <= r) ++k;
         const int y = R.y0[k] + (r - R.first_row[k]);
         float *row = f + (long long)y * pitch + R.x0[k];
-        for (int x = threadIdx.x; x < R.w[k]; x += blockDim.x) row[x] = 0.0f;
+        const int w = R.w[k];
+        if ((reinterpret_cast<uintptr_t>(row) & 15) == 0 && (w & 3) == 0) {
+            float4 *row4 = reinterpret_cast<float4 *>(row);
+            for (int x = threadIdx.x; x < (w >> 2); x += blockDim.x) row4[x] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            for (int x = threadIdx.x; x < w; x += blockDim.x) row[x] = 0.0f;
+        }
     }
 }
 

@@ -45,8 +45,16 @@ Wavelet make_wavelet(int id, bool inverse)
 
 namespace {
 
-template <int NS, bool INV>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+// Test hook: one warp runs the ordered wait of segment 0 of a forward
+// 1024 x 1024 level whose counters (order, zeroed by the caller) nothing
+// advances; the wait gives up after `limit` polls and raises the error word.
+__global__ void order_wait_timeout_kernel(LevelDesc D, uint32_t limit, int *err)
+{
+    units::order_wait(D, false, 2, 0, threadIdx.x & 31, err, limit);
+}
+
+template <int NS, bool INV, bool ORD>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, ORD ? 5 : 0)
 level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant__ LevelMaps M)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -59,14 +67,34 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
     const bool fast_launch = units::fast_ok<INV>(D);
     // tensor copies need 128-byte aligned slots
     const bool maps = INV && D.tmap && (smem_addr(smem) & 127) == 0;
-    const CUtensorMap *mll = maps ? &M.ll : nullptr, *mfr = maps ? &M.frame : nullptr;
+    const LevelMaps *mp = maps ? &M : nullptr;
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
-    for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
-        const int q = u / D.n_strips;
-        const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
-        if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mll, mfr))
-            break;
+    if constexpr (ORD) {
+        // ordered in-place launch: tickets in segment order; a unit waits
+        // (after issuing its first loads, before its first store) only for
+        // units holding earlier tickets, which are running; it takes the
+        // next ticket a few stages before its end
+        int next = 0;
+        if (lane == 0) next = atomicAdd(D.order, 1);
+        for (;;) {
+            const int u = __shfl_sync(0xffffffffu, next, 0);
+            if (u >= n) break;
+            const int q = u / D.n_strips;
+            const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
+            next = n;
+            if (!units::run_unit<NS, INV, true>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp,
+                                                &next))
+                break;
+            units::order_done(D, seg, lane);
+        }
+    } else {
+        for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
+            const int q = u / D.n_strips;
+            const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
+            if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp))
+                break;
+        }
     }
 }
 
@@ -103,34 +131,64 @@ bool encode_band_map(CUtensorMap *m, const float *base, long long w, long long h
 }
 
 // Tensor maps of an inverse level: LL from in[0], and the frame the other
-// three bands live in (HL at +ws, LH at +hs rows, HH at both), when the
-// bands sit in one frame as the level pipeline lays them out.
-bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w)
+// three bands live in -- HL at column dx, LH at row dy, HH at both, as the
+// level pipeline lays them out (dx, dy = the band's half sizes) or as a
+// zero-padded sparse frame does (the outer midpoints); an ordered in-place
+// level reads HL and the staged LH / HH rows from one frame and the other
+// LH / HH rows from the caller's (`lower`).  Fills dx, dy.
+bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w, int &dx, int &dy)
 {
     if (d.rows_only || d.h < 2 || d.w < 2) return false;
-    const long long ws = (d.w + 1) / 2, hs = (d.h + 1) / 2, p = d.in_pitch[2];
-    if (d.in_pitch[1] != p || d.in_pitch[3] != p) return false;
-    const float *frame = d.in[2] - hs * p;
-    if (d.in[1] != frame + ws || d.in[3] != frame + hs * p + ws) return false;
-    return encode_band_map(&M.ll, d.in[0], ws, hs, d.in_pitch[0], box_w) &&
-           encode_band_map(&M.frame, frame, d.w, d.h, p, box_w);
+    const long long ws = (d.w + 1) / 2, hs = (d.h + 1) / 2, hx = d.w / 2, hy = d.h / 2;
+    // the H columns' offset: HH sits dx floats right of LH in the same rows
+    const long long sx = d.order ? d.alt[1] - d.alt[0] : d.in[3] - d.in[2];
+    if (sx < ws || (d.order && d.in[3] - d.in[2] != sx)) return false;
+    const long long p = d.in_pitch[1];
+    const float *frame = d.in[1] - sx;
+    const float *lh = d.order ? d.alt[0] : d.in[2];
+    if ((d.order ? d.alt_pitch : d.in_pitch[2]) != p || (!d.order && d.in_pitch[3] != p)) return false;
+    const long long off = lh - frame;
+    if (off < 0 || off % p != 0 || off / p < hs) return false;
+    const long long sy = off / p;
+    if (sx + hx > INT32_MAX || sy + hy > INT32_MAX) return false;
+    const long long fw = sx + hx, fh = sy + hy;
+    bool ok = encode_band_map(&M.ll, d.in[0], ws, hs, d.in_pitch[0], box_w) &&
+              encode_band_map(&M.frame, frame, fw, fh, p, box_w);
+    if (ok && d.order) {
+        const long long q = d.in_pitch[2];
+        if (d.in_pitch[3] != q) return false;
+        const float *lower = d.in[2] - sy * q;
+        ok = encode_band_map(&M.lower, lower, fw, fh, q, box_w);
+    }
+    dx = int(sx);
+    dy = int(sy);
+    return ok;
 }
 
-template <int NS, bool INV>
-cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
+template <int NS, bool INV, bool ORD>
+cudaError_t launch_o(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
 {
     // once per instantiation, safe from several host threads
     static const cudaError_t configured =
-        cudaFuncSetAttribute(level_kernel<NS, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+        cudaFuncSetAttribute(level_kernel<NS, INV, ORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (configured != cudaSuccess) return configured;
     const int units = d.n_strips * d.n_segs;
     const int grid = ceil_div(units, kWarpsPerCta);
     LevelMaps M;
     memset(&M, 0, sizeof(M));
     LevelDesc dd = d;
-    dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M, kBandRowF)) ? 1 : 0;
-    return launch_pdl(level_kernel<NS, INV>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W, err,
-                      M);
+    int dx = 0, dy = 0;
+    dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M, kBandRowF, dx, dy)) ? 1 : 0;
+    dd.map_dx = dx;
+    dd.map_dy = dy;
+    return launch_pdl(level_kernel<NS, INV, ORD>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W,
+                      err, M);
+}
+
+template <int NS, bool INV>
+cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
+{
+    return d.order ? launch_o<NS, INV, true>(d, W, stream, err) : launch_o<NS, INV, false>(d, W, stream, err);
 }
 
 }  // namespace
@@ -193,6 +251,27 @@ void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse)
     seg = std::min(seg, std::max(npairs, 1));
     d.seg_pairs = seg;
     d.n_segs = ceil_div(npairs, seg);
+}
+
+int order_wait_timeout_words()
+{
+    LevelDesc d{};
+    d.w = d.h = 1024;
+    plan_level(d, 0, false);
+    return d.n_segs + 1;
+}
+
+cudaError_t launch_order_wait_timeout(uint32_t limit, int *order, int *err, cudaStream_t stream)
+{
+    LevelDesc d{};
+    d.w = d.h = 1024;
+    plan_level(d, 0, false);
+    d.order = order;
+    d.stage_seg = d.n_segs;
+    d.order_dy = (d.h + 1) / 2;
+    d.reverse = 1;
+    order_wait_timeout_kernel<<<1, 32, 0, stream>>>(d, limit, err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_level(const LevelDesc &d, int wavelet, bool inverse, cudaStream_t stream, int *err)

@@ -42,22 +42,87 @@ struct LevelDesc {
     int reverse;   // hand out the segments bottom-up (the previous level ended there)
     int rows_only;
     int tmap;      // inverse: the tensor maps of the launch are valid (set by launch_level)
+    int map_dx, map_dy;  // with tmap: column of HL / HH and row of LH / HH in the mapped frames
     const float *in[4];
     long long in_pitch[4];
     float *out[4];
     long long out_pitch[4];
+    // Ordered in-place launch (level 0 of a transform in the caller's frame;
+    // null otherwise).  Units are handed out by a ticket in segment order
+    // (bottom-up when reverse is set) and each one waits, before it starts,
+    // for the segments that come earlier in that order and read the rows it
+    // overwrites (inplace_readers).  order[0] is the ticket and order[1 + s]
+    // counts the finished strips of segment s; all zero at launch.
+    int *order;
+    // Segments >= stage_seg write (forward) or read (inverse) their LH and
+    // HH rows at alt[0] / alt[1] (pitch alt_pitch) instead of out / in.
+    int stage_seg;
+    int order_dy;  // frame row of the LH / HH bands' first row ((h + 1) / 2 in a dense frame)
+    float *alt[2];
+    long long alt_pitch;
 };
 
+__host__ __device__ inline int floordiv_i(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+__host__ __device__ inline int min_i(int a, int b) { return a < b ? a : b; }
+__host__ __device__ inline int max_i(int a, int b) { return a > b ? a : b; }
+
+// The segments of an ordered in-place level of height h (segments of S row
+// pairs, nsegs of them, lifting latency lat pairs; the LH / HH bands from
+// frame row dy on) that must be finished before segment s writes into the
+// caller's frame: the inclusive range [a, b], empty when b < a.
+//   forward: every segment whose image rows (its pairs k0 - lat .. k1 + lat,
+//     mirrored) meet the LH / HH rows dy + k0 .. that s writes; a staged
+//     segment (s >= stage_seg) writes those rows elsewhere and waits for
+//     nothing.
+//   inverse: every segment below stage_seg (the ones reading LH / HH in the
+//     frame) whose LH / HH rows meet the image rows 2 k0 .. 2 k1 - 1 that s
+//     writes.
+// Each read range is widened by two rows of margin.  The host chooses
+// stage_seg so that every segment in range comes earlier in the launch's
+// order than s.
+__host__ __device__ inline void inplace_readers(int h, int S, int nsegs, int lat, bool inverse, int s,
+                                                int stage_seg, int dy, int &a, int &b)
+{
+    constexpr int mg = 2;
+    const int hs = (h + 1) >> 1;
+    const int k0 = s * S, k1 = min_i(k0 + S, hs);
+    a = 1;
+    b = 0;
+    if (!inverse) {
+        if (s >= stage_seg) return;
+        const int lo = dy + k0, hi = dy + min_i(k1, h >> 1);
+        if (hi <= lo) return;
+        // segment s' reads rows [2 (s' S - lat) - mg, 2 ((s' + 1) S + lat + 1) + mg)
+        a = max_i(0, floordiv_i(lo - 2 * lat - 2 - mg, 2 * S));
+        b = min_i(nsegs - 1, floordiv_i(hi + 2 * lat + mg + 2 * S - 1, 2 * S) - 1);
+    } else {
+        const int lo = 2 * k0, hi = min_i(2 * k1, h);
+        if (hi <= lo) return;
+        // segment s' reads rows dy + [s' S - lat - mg, (s' + 1) S + lat + 1 + mg)
+        a = max_i(0, floordiv_i(lo - dy - lat - 1 - mg, S));
+        b = min_i(min_i(nsegs, stage_seg) - 1, floordiv_i(hi - dy + lat + mg + S - 1, S) - 1);
+    }
+}
+
 // Tensor maps of an inverse level: the LL band (box kBandRowF x 2) and the
-// coefficient frame holding HL, LH, HH (the level's w x h region, same box).
+// coefficient frame holding HL, LH, HH (the level's w x h region, same box);
+// in an ordered in-place launch `frame` is the staging frame (HL and the
+// staged LH, HH rows) and `lower` the caller's frame.
 struct LevelMaps {
     CUtensorMap ll;
     CUtensorMap frame;
+    CUtensorMap lower;  // ordered in-place launches: the frame holding the in-frame LH, HH rows
 };
 
 // Fills n_strips / seg_pairs / n_segs for a level of size w x h (the
 // segment length depends on the direction).
 void plan_level(LevelDesc &d, int seg_pairs_hint, bool inverse);
+
+// Test hook of the ordered in-place wait: counters needed (ints, zeroed by
+// the caller) and the launch of one warp whose wait gives up after `limit`
+// polls, raising kErrQueueTimeout into err.
+int order_wait_timeout_words();
+cudaError_t launch_order_wait_timeout(uint32_t limit, int *order, int *err, cudaStream_t stream);
 
 // Launch one level on `stream`.  err: device error word (may be null).
 cudaError_t launch_level(const LevelDesc &d, int wavelet, bool inverse, cudaStream_t stream,

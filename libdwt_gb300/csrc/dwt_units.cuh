@@ -298,6 +298,65 @@ struct WarpPipe {
     __device__ __forceinline__ void release(uint32_t, int) const { __syncwarp(); }
 };
 
+// Ordered in-place launches (LevelDesc::order).  order_wait: the warp waits
+// (at most `limit` polls, 128 ns apart, each lane polling one segment; it
+// gives up early when another warp has raised an error) until every strip
+// of the segments that must finish before segment `seg` writes into the
+// frame is done.  order_done: counts a
+// finished strip of `seg`; every read of the unit has completed (its stages
+// were waited for), which is all a later writer of those rows needs.
+// order_ticket: lane 0 takes the warp's next ticket.
+constexpr uint32_t kOrderWaitLimit = 1u << 24;
+
+__device__ __forceinline__ bool order_wait(const LevelDesc &D, bool inverse, int lat, int seg, int lane, int *err,
+                                           uint32_t limit = kOrderWaitLimit)
+{
+    int a, b;
+    inplace_readers(D.h, D.seg_pairs, D.n_segs, lat, inverse, seg, D.stage_seg, D.order_dy, a, b);
+    if (b < a) return true;
+    // one segment per lane (ranges span a few segments; longer ones loop)
+    bool ok = true;
+    for (int r0 = a; r0 <= b; r0 += 32) {
+        const int r = r0 + lane;
+        bool mine = r > b || r == seg;  // the host's stage_seg excludes seg itself
+        uint32_t spins = 0;
+        while (!__all_sync(0xffffffffu, mine)) {
+            if (!mine) mine = ld_acquire(D.order + 1 + r) >= D.n_strips;
+            if (__all_sync(0xffffffffu, mine)) break;
+            __nanosleep(128);
+            const bool give_up = ++spins > limit || (err && *reinterpret_cast<volatile int *>(err) != 0);
+            if (__any_sync(0xffffffffu, give_up)) {
+                if (lane == 0) raise_error(err, kErrQueueTimeout);
+                ok = false;
+                break;
+            }
+        }
+        if (!ok) break;
+    }
+    __syncwarp();
+    return ok;
+}
+
+__device__ __forceinline__ void order_done(const LevelDesc &D, int seg, int lane)
+{
+    __syncwarp();
+    if (lane == 0) atomicAdd(D.order + 1 + seg, 1);
+}
+
+__device__ __forceinline__ void order_ticket(const LevelDesc &D, int lane, int *next)
+{
+    if (lane == 0) *next = atomicAdd(D.order, 1);
+}
+
+// Waits (bounded) for the first `count` stages a unit has issued, so that
+// no copy is still landing in the ring when the unit gives up.
+template <class Pipe>
+__device__ __forceinline__ void drain_issued(const Pipe &pipe, uint32_t t0, int count)
+{
+    for (int u = 0; u < count; ++u) pipe.wait(t0 + u);
+    __syncwarp();
+}
+
 // Stage count of a 2D unit of segment `seg`: pairs k0-LAT .. k1+LAT-1, two
 // per stage.
 template <int NS>
@@ -318,9 +377,9 @@ __device__ __forceinline__ void unit_span(const LevelDesc &D, int seg, int &k0, 
 // path for strips touching the left or right border (mirrored columns,
 // partial lanes) or unaligned outputs.  The rows are staged from column B
 // on, `win` columns wide, `slot_f` floats per row slot.
-template <int NS, bool EDGE, class Pipe>
+template <int NS, bool EDGE, class Pipe, bool ORD = false>
 __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
-                             int win, int slot_f, uint32_t &tick, int lane, int *err)
+                             int win, int slot_f, uint32_t &tick, int lane, int *err, int *next = nullptr)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
@@ -367,6 +426,12 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     if (pipe.producer(lane))
         for (int u = 0; u < min(iters, Pipe::kDepth) && issued_ok; ++u) issued_ok = issue(u);
     __syncwarp();
+    // ordered in-place launch: the reads are in flight; wait before storing
+    if (ORD && !order_wait(D, false, LAT, seg, lane, err)) {
+        drain_issued(pipe, t0, issued_ok ? min(iters, Pipe::kDepth) : 0);
+        return false;
+    }
+    const int ticket_at = max(0, iters - Pipe::kDepth);
 
     // packed constants
     f2 C[4];
@@ -381,10 +446,13 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     const bool vL0 = lane_ok && c0 < w, vH0 = lane_ok && c0 + 1 < w;
     const bool vL1 = lane_ok && c0 + 2 < w, vH1 = lane_ok && c0 + 3 < w;
     const int q = (b >> 1) + 2 * lane;
+    // LH / HH of a staged segment of an ordered in-place launch go to alt
+    const bool alt = ORD && seg >= D.stage_seg;
+    const long long sLH = alt ? D.alt_pitch : D.out_pitch[2], sHH = alt ? D.alt_pitch : D.out_pitch[3];
     float *pLL = D.out[0] + q + (long long)k0 * D.out_pitch[0];
     float *pHL = D.out[1] + q + (long long)k0 * D.out_pitch[1];
-    float *pLH = D.out[2] + q + (long long)k0 * D.out_pitch[2];
-    float *pHH = D.out[3] + q + (long long)k0 * D.out_pitch[3];
+    float *pLH = (alt ? D.alt[0] : D.out[2]) + q + (long long)k0 * sLH;
+    float *pHH = (alt ? D.alt[1] : D.out[3]) + q + (long long)k0 * sHH;
     const int last_h = (h >> 1) - 1;  // last output pair with an H row
 
     f2 e[2] = {0, 0}, o[2] = {0, 0}, o1[2] = {0, 0}, e1[2] = {0, 0}, o2[2] = {0, 0};
@@ -414,6 +482,7 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
         pipe.release(t0 + u, lane);
         if (pipe.producer(lane) && issued_ok && u >= Pipe::kLag && u - Pipe::kLag + Pipe::kDepth < iters)
             issued_ok = issue(u - Pipe::kLag + Pipe::kDepth);
+        if (ORD && u == ticket_at) order_ticket(D, lane, next);
         // rows: horizontal lifting (a single-sample row is only scaled)
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -453,8 +522,8 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                 }
                 pLL += D.out_pitch[0];
                 pHL += D.out_pitch[1];
-                pLH += D.out_pitch[2];
-                pHH += D.out_pitch[3];
+                pLH += sLH;
+                pHH += sHH;
             }
         }
     }
@@ -609,14 +678,15 @@ __device__ __forceinline__ void v_inverse2(f2 A, f2 B, f2 &o, f2 &e1, f2 &o1, f2
 // band column B/2 on, `band_win` columns wide.  Stage layout: band k (LL,
 // HL, LH, HH) at slot + k*kBandSlotF, its row for pair r at + r*kBandRowF,
 // band column c at offset c - (window start rounded down to 16 bytes).
-// With tensor maps (mll: LL band, mfr: the frame holding HL, LH, HH), an
+// With tensor maps (maps: the LL band, the frame holding HL, LH, HH and, in
+// an ordered in-place launch, the frame holding the in-frame LH, HH rows), an
 // interior unit stages each band's two consecutive rows of a stage with one
-// 68 x 2 box copy; stages with mirrored rows and edge units use one bulk
-// copy per band row.
-template <int NS, bool EDGE, class Pipe>
+// 68 x 2 box copy; stages with mirrored rows and edge units use one bulk copy
+// per band row.
+template <int NS, bool EDGE, class Pipe, bool ORD = false>
 __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
-                             int band_win, const CUtensorMap *mll, const CUtensorMap *mfr, uint32_t &tick,
-                             int lane, int *err)
+                             int band_win, const LevelMaps *maps, uint32_t &tick, int lane, int *err,
+                             int *next = nullptr)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
@@ -633,15 +703,18 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     // because source pitches are multiples of 4 floats
     const int loL = max(bqB, 0), hiL = min(bqB + band_win, Lw);
     const int loH = loL, hiH = min(bqB + band_win, Hw);
+    // LH / HH of a staged segment of an ordered in-place launch come from alt
+    const bool alt = ORD && seg >= D.stage_seg;
     BandIn iLL, iHL, iLH, iHH;
     iLL.init(D.in[0], D.in_pitch[0], loL, hiL - loL);
     iHL.init(D.in[1], D.in_pitch[1], loH, hiH - loH);
-    iLH.init(D.in[2], D.in_pitch[2], loL, hiL - loL);
-    iHH.init(D.in[3], D.in_pitch[3], loH, hiH - loH);
+    iLH.init(alt ? D.alt[0] : D.in[2], alt ? D.alt_pitch : D.in_pitch[2], loL, hiL - loL);
+    iHH.init(alt ? D.alt[1] : D.in[3], alt ? D.alt_pitch : D.in_pitch[3], loH, hiH - loH);
     const uint32_t tx1 = 2 * (iLL.bytes + iHL.bytes + iLH.bytes + iHH.bytes);
     // box copies: interior units only (their windows start at or after
     // column 0 and the box's 16-byte aligned x is that window start)
-    const bool boxes = !EDGE && mll != nullptr && mfr != nullptr;
+    const bool boxes = !EDGE && maps != nullptr;
+    const bool lower = ORD && !alt;  // LH / HH boxes from maps->lower
     constexpr uint32_t kBoxBytes = kBandRowF * 2 * 4;
 
     // this lane's offsets inside a stage: even samples from the L bands
@@ -682,10 +755,11 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
         if (boxes && m >= 0 && 2 * m + 3 < h) {
             // both pairs interior: band rows m and m + 1 of every band
             mbar_arrive_expect_tx(bar, 4 * kBoxBytes);
-            tma_load_2d(slot, mll, loL - iLL.shift, m, bar);
-            tma_load_2d(slot + kBandSlotF, mfr, Lw + loH - iHL.shift, m, bar);
-            tma_load_2d(slot + 2 * kBandSlotF, mfr, loL - iLH.shift, hs + m, bar);
-            tma_load_2d(slot + 3 * kBandSlotF, mfr, Lw + loH - iHH.shift, hs + m, bar);
+            const CUtensorMap *mlo = lower ? &maps->lower : &maps->frame;
+            tma_load_2d(slot, &maps->ll, loL - iLL.shift, m, bar);
+            tma_load_2d(slot + kBandSlotF, &maps->frame, D.map_dx + loH - iHL.shift, m, bar);
+            tma_load_2d(slot + 2 * kBandSlotF, mlo, loL - iLH.shift, D.map_dy + m, bar);
+            tma_load_2d(slot + 3 * kBandSlotF, mlo, D.map_dx + loH - iHH.shift, D.map_dy + m, bar);
             return true;
         }
         mbar_arrive_expect_tx(bar, tx1);
@@ -707,6 +781,12 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     if (pipe.producer(lane))
         for (int u = 0; u < min(iters, Pipe::kDepth) && issued_ok; ++u) issued_ok = issue(u);
     __syncwarp();
+    // ordered in-place launch: the reads are in flight; wait before storing
+    if (ORD && !order_wait(D, true, LAT, seg, lane, err)) {
+        drain_issued(pipe, t0, issued_ok ? min(iters, Pipe::kDepth) : 0);
+        return false;
+    }
+    const int ticket_at = max(0, iters - Pipe::kDepth);
 
     f2 C[4];
 #pragma unroll
@@ -752,6 +832,7 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
         pipe.release(t0 + u, lane);
         if (pipe.producer(lane) && issued_ok && u >= Pipe::kLag && u - Pipe::kLag + Pipe::kDepth < iters)
             issued_ok = issue(u - Pipe::kLag + Pipe::kDepth);
+        if (ORD && u == ticket_at) order_ticket(D, lane, next);
         // rows first (src/libdwt.c:6706-6717), then columns
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -805,20 +886,26 @@ __device__ __forceinline__ bool fast_ok(const LevelDesc &D)
             const uintptr_t a = reinterpret_cast<uintptr_t>(D.in[k]);
             ok = ok && ((a & 7) == 0) && ((D.in_pitch[k] & 3) == 0);
         }
+        if (D.order)
+            for (int k = 0; k < 2; ++k)
+                ok = ok && ((reinterpret_cast<uintptr_t>(D.alt[k]) & 7) == 0) && ((D.alt_pitch & 3) == 0);
     } else {
         ok = true;
         for (int k = 0; k < 4; ++k)
             ok = ok && ((reinterpret_cast<uintptr_t>(D.out[k]) & 7) == 0) && ((D.out_pitch[k] & 1) == 0);
+        if (D.order)
+            for (int k = 0; k < 2; ++k)
+                ok = ok && ((reinterpret_cast<uintptr_t>(D.alt[k]) & 7) == 0) && ((D.alt_pitch & 1) == 0);
     }
     return ok;
 }
 
 // Runs one unit (strip, seg) of the level described by D on a warp's
 // private ring.
-template <int NS, bool INV>
+template <int NS, bool INV, bool ORD = false>
 __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
                                          uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch,
-                                         const CUtensorMap *mll = nullptr, const CUtensorMap *mfr = nullptr)
+                                         const LevelMaps *maps = nullptr, int *next = nullptr)
 {
     if (D.h == 1 || D.rows_only)
         return INV ? inverse_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err)
@@ -827,10 +914,14 @@ __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, i
     const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
     const WarpPipe pipe{ring, bars};
     if (INV)
-        return edge ? inverse_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn / 2, mll, mfr, tick, lane, err)
-                    : inverse_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn / 2, mll, mfr, tick, lane, err);
-    return edge ? forward_unit<NS, true>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err)
-                : forward_unit<NS, false>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err);
+        return edge ? inverse_unit<NS, true, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn / 2, maps, tick, lane,
+                                                            err, next)
+                    : inverse_unit<NS, false, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn / 2, maps, tick,
+                                                             lane, err, next);
+    return edge ? forward_unit<NS, true, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err,
+                                                        next)
+                : forward_unit<NS, false, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane,
+                                                         err, next);
 }
 
 // Per-warp ring and barriers inside a CTA's dynamic shared memory.

@@ -41,3 +41,26 @@ def test_wait_that_runs_out_reports_and_the_context_survives(L, capfd):
     assert np.array_equal(buf, ref)
     assert L.dwt_gpu_get_last_error() == 0
     assert L.dwt_gpu_sync_check() == 0
+
+
+def test_inplace_wait_invalid_limit_is_refused(L):
+    L.dwt_gpu_selftest_inplace_wait_timeout.argtypes = [C.c_int]
+    assert L.dwt_gpu_selftest_inplace_wait_timeout(0) == -1
+
+
+@pytest.mark.gpu
+def test_inplace_order_wait_that_runs_out_reports(L, capfd):
+    """The wait of an ordered in-place unit for earlier segments that never
+    finish gives up, raises its code (2) and leaves the context usable."""
+    import libdwt_gb300 as D
+    L.dwt_gpu_selftest_inplace_wait_timeout.argtypes = [C.c_int]
+    rc = L.dwt_gpu_selftest_inplace_wait_timeout(2000)
+    err = capfd.readouterr().err
+    assert rc == -4  # DWT_GPU_EDEVICE
+    assert "device-side wait gave up (code 2)" in err
+    rng = np.random.default_rng(4)
+    img = rng.integers(0, 256, size=(260, 301)).astype(np.float32)
+    ref, j = O.transform2_dense(img, "cdf53", "f", -1)
+    buf = img.copy()
+    assert D.transform2(buf, "cdf53", "f", 301 * 4, 4, (301, 260), (301, 260), -1) == j
+    assert np.array_equal(buf, ref)

@@ -1,6 +1,6 @@
 """The drop-in 2D calls (dwt_cdf{97,53}_2{f,i}_s) on dense device frames of
-1 Mpx and more, which run in place with level 0 in row bands that stage only
-the HL quadrant and the rows no band order can protect: bit-exact against the oracle for square, odd and pitched frames,
+1 Mpx and more, which run in place with level 0 as one ordered launch that
+stages only the HL quadrant and the last segments of its order: bit-exact against the oracle for square, odd and pitched frames,
 every sample of a row's padding (pitch > width) untouched, and the same on the
 full-size 16384 x 16384 image."""
 import numpy as np
@@ -72,9 +72,10 @@ def test_inplace_device_fullsize(env):
         assert np.array_equal(dev.cpu().numpy(), ref_i), f"{wav} inverse differs"
 
 
-def test_inplace_device_band_counts():
-    """The same frames with 3, 8 and 16 row bands for the in-place level 0
-    (DWT_GPU_INPLACE_BANDS, read once per process: child processes)."""
+def test_inplace_device_leads():
+    """The same frames with no lead and with a long one before the ordered
+    level 0's staged segments (DWT_GPU_INPLACE_LEAD, read once per process:
+    child processes)."""
     import os
     import subprocess
     import sys
@@ -85,8 +86,8 @@ def test_inplace_device_band_counts():
             "import test_gpu_inplace_device as T\n"
             "env = (D, torch, synth)\n"
             "for c in T.CASES[:5]: T.test_inplace_device_matches_oracle(env, *c)\n"
-            "print('bands ok')\n") % (root, os.path.join(root, "tests"))
-    for bands in ("3", "8", "16"):
+            "print('leads ok')\n") % (root, os.path.join(root, "tests"))
+    for lead in ("0", "40"):
         r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=900,
-                           env=dict(os.environ, DWT_GPU_INPLACE_BANDS=bands))
-        assert r.returncode == 0 and "bands ok" in r.stdout, r.stdout + r.stderr
+                           env=dict(os.environ, DWT_GPU_INPLACE_LEAD=lead))
+        assert r.returncode == 0 and "leads ok" in r.stdout, r.stdout + r.stderr
