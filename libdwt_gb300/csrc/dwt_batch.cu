@@ -132,7 +132,9 @@ __device__ __forceinline__ bool level_item(const BatchImage &I, int level, int u
     const LevelDesc D = level_desc(I, level);
     const Wavelet W = make_wavelet_dev(I.wavelet, INV);
     const int strip = unit % D.n_strips, seg = unit / D.n_strips;
-    return units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, units::fast_ok<INV>(D));
+    int unused = 0;
+    return units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, units::fast_ok<INV>(D), nullptr,
+                                    unused);
 }
 
 __global__ void __launch_bounds__(kBatchWarps * 32)

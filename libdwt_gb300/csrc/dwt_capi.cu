@@ -863,10 +863,10 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
     // the HL quadrant and the staged LH / HH rows between the frame and T
     auto copy_staged = [&](float *dst, long long dp, const float *src, long long sp) -> cudaError_t {
         cudaError_t e = cudaSuccess;
-        if (W > ws) e = launch_copy_rows_dev(dst + ws, dp * 4, src + ws, sp * 4, (W - ws) * 4LL, hs, s2);
+        if (W > ws) e = launch_copy_rows_bulk(dst + ws, dp * 4, src + ws, sp * 4, (W - ws) * 4LL, hs, s2, c.d_err);
         if (e == cudaSuccess && staged_lo < H)
-            e = launch_copy_rows_dev(dst + staged_lo * dp, dp * 4, src + staged_lo * sp, sp * 4, W * 4LL,
-                                      H - staged_lo, s2);
+            e = launch_copy_rows_bulk(dst + staged_lo * dp, dp * 4, src + staged_lo * sp, sp * 4, W * 4LL,
+                                      H - staged_lo, s2, c.d_err);
         return e;
     };
     CK(cudaMemsetAsync(order.p, 0, size_t(nsegs + 1) * 4, s));
@@ -1025,7 +1025,8 @@ static int sparse_inplace(Lane &c, int wavelet, bool inverse, float *F, long lon
         cudaError_t e = cudaSuccess;
         auto rect = [&](int x0, long long y0, int w, long long h) {
             if (e == cudaSuccess && w > 0 && h > 0)
-                e = launch_copy_rows_dev(dst + y0 * dp + x0, dp * 4, src + y0 * sp + x0, sp * 4, w * 4LL, h, s2);
+                e = launch_copy_rows_bulk(dst + y0 * dp + x0, dp * 4, src + y0 * sp + x0, sp * 4, w * 4LL, h, s2,
+                                          c.d_err);
         };
         const long long rows = (long long)ody + hy - staged_lo;
         rect(odx, 0, hx, ly);             // HL

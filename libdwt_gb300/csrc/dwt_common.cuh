@@ -244,6 +244,24 @@ __device__ __forceinline__ void fence_proxy_async_global()
     asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
+// TMA bulk copy shared -> global in the thread's bulk async-group; commit
+// closes the group; wait_read<N> waits until at most N groups still read
+// shared memory; wait_all until every group has completed its writes.
+// Addresses 16-byte aligned, sizes multiples of 16 bytes.
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read()
+{
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Error codes raised by device code into the error word.
 enum DeviceError : int {
     kErrNone = 0,

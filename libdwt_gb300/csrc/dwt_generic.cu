@@ -352,6 +352,87 @@ int grid_for(long long n, int block)
     return int(g);
 }
 
+// Device-to-device copy of `rows` rows of `width` bytes by one warp per
+// block through a small ring of shared-memory buffers with TMA bulk copies
+// (kBulkBufs - 1 loads in flight), so that a block fits beside level kernels
+// that fill an SM's registers and most of its shared memory: a copy on
+// another stream then streams during the latency-bound smaller levels
+// instead of waiting for free SM slots.  Every 16-byte aligned; waits are
+// bounded (the error word on a timeout, after which the block only drains
+// its stores).
+constexpr int kBulkBufs = 4;
+constexpr int kBulkPiece = 4096;  // bytes per buffer
+constexpr int kBulkSmem = kBulkBufs * kBulkPiece + kBulkBufs * 8;
+
+__global__ void __launch_bounds__(32) bulk_copy_rows_kernel(const unsigned char *src, long long spitch,
+                                                            unsigned char *dst, long long dpitch, long long width,
+                                                            long long rows, int *err)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBulkBufs * kBulkPiece);
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+        for (int b = 0; b < kBulkBufs; ++b) mbar_init(&bar[b], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const long long per_row = (width + kBulkPiece - 1) / kBulkPiece;
+    const long long total = per_row * rows;
+    // this block's pieces: blockIdx.x, + gridDim.x, ...; i-th of them
+    auto piece = [&](long long i, const unsigned char *&s, unsigned char *&d, uint32_t &bytes) {
+        const long long c = blockIdx.x + i * gridDim.x;
+        const long long r = c / per_row, off = (c % per_row) * kBulkPiece;
+        s = src + r * spitch + off;
+        d = dst + r * dpitch + off;
+        bytes = uint32_t(width - off < kBulkPiece ? width - off : kBulkPiece);
+    };
+    const long long mine = total > blockIdx.x ? (total - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    auto load = [&](long long i) {
+        const unsigned char *s;
+        unsigned char *d;
+        uint32_t bytes;
+        piece(i, s, d, bytes);
+        const int b = int(i % kBulkBufs);
+        mbar_arrive_expect_tx(&bar[b], bytes);
+        bulk_g2s(sm + b * kBulkPiece, s, bytes, &bar[b]);
+    };
+    long long issued = mine < kBulkBufs - 1 ? mine : kBulkBufs - 1;
+    if (lane == 0)
+        for (long long i = 0; i < issued; ++i) load(i);
+    __syncwarp();
+    for (long long i = 0; i < mine; ++i) {
+        const int b = int(i % kBulkBufs);
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(&bar[b], uint32_t(i / kBulkBufs) & 1u))) {
+            // give up: raise the error and wait (bounded) for the loads still
+            // in flight before the block's shared memory goes away
+            if (lane == 0) {
+                if (err) atomicCAS(err, 0, int(kErrWaitTimeout));
+                for (long long j = i; j < issued; ++j)
+                    mbar_wait_bounded(&bar[j % kBulkBufs], uint32_t(j / kBulkBufs) & 1u);
+            }
+            break;
+        }
+        if (lane == 0) {
+            const unsigned char *s;
+            unsigned char *d;
+            uint32_t bytes;
+            piece(i, s, d, bytes);
+            fence_proxy_async_smem();
+            bulk_s2g(d, sm + b * kBulkPiece, bytes);
+            bulk_commit();
+            if (issued < mine) {
+                // the buffer of piece `issued` was read by the store of piece
+                // i - 1: at most the store just issued may still read
+                bulk_wait_read<1>();
+                load(issued++);
+            }
+        }
+        issued = __shfl_sync(0xffffffffu, issued, 0);
+    }
+    if (lane == 0) bulk_wait_all();
+    __syncwarp();
+}
+
 }  // namespace
 
 cudaError_t launch_repack(const void *src, long long sx, long long sy, int ox, int oy, float *dst,
@@ -389,6 +470,30 @@ cudaError_t launch_copy_rows_dev(void *dst, long long dpitch, const void *src, l
         return 8 * sms;
     }();
     return launch_copy_rows_ctas(dst, dpitch, src, spitch, width, rows, s, ctas);
+}
+
+cudaError_t launch_copy_rows_bulk(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                  long long rows, cudaStream_t s, int *err)
+{
+    if (width <= 0 || rows <= 0) return cudaSuccess;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
+                        uintptr_t(dpitch) | uintptr_t(spitch) | uintptr_t(width);
+    if ((a & 15) != 0) return launch_copy_rows_dev(dst, dpitch, src, spitch, width, rows, s);
+    // 4 blocks per SM: one fits beside a full level kernel, the others run
+    // as the level kernels drain
+    static const int ctas = [] {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
+        const char *e = getenv("DWT_GPU_BULK_COPY_CTAS");
+        const int v = e ? atoi(e) : 0;
+        return (v > 0 && v <= 32 ? v : 4) * sms;
+    }();
+    const long long pieces = (width + kBulkPiece - 1) / kBulkPiece * rows;
+    const int grid = int(std::min<long long>(pieces, ctas));
+    bulk_copy_rows_kernel<<<grid, 32, kBulkSmem, s>>>(static_cast<const unsigned char *>(src), spitch,
+                                                     static_cast<unsigned char *>(dst), dpitch, width, rows, err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_copy_rows_ctas(void *dst, long long dpitch, const void *src, long long spitch, long long width,

@@ -21,6 +21,12 @@ cudaError_t launch_copy_rows(void *dst, long long dpitch, const void *src, long 
 // copy engines move 2D device-to-device copies far slower).
 cudaError_t launch_copy_rows_dev(void *dst, long long dpitch, const void *src, long long spitch, long long width,
                                  long long rows, cudaStream_t s);
+// The same through TMA bulk copies by one-warp blocks with 16 KB of shared
+// memory, which fit beside full level kernels (a copy on a second stream);
+// 16-byte aligned frames only, else launch_copy_rows_dev.  err: device error
+// word of a bounded wait that gave up (may be null).
+cudaError_t launch_copy_rows_bulk(void *dst, long long dpitch, const void *src, long long spitch, long long width,
+                                  long long rows, cudaStream_t s, int *err);
 cudaError_t launch_copy_rows_ctas(void *dst, long long dpitch, const void *src, long long spitch, long long width,
                                   long long rows, cudaStream_t s, int ctas);
 

@@ -71,28 +71,37 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
     uint32_t tick = 0;
     const int n = D.n_strips * D.n_segs;
     if constexpr (ORD) {
-        // ordered in-place launch: tickets in segment order; a unit waits
-        // (after issuing its first loads, before its first store) only for
-        // units holding earlier tickets, which are running; it takes the
-        // next ticket a few stages before its end
-        int next = 0;
-        if (lane == 0) next = atomicAdd(D.order, 1);
-        for (;;) {
-            const int u = __shfl_sync(0xffffffffu, next, 0);
-            if (u >= n) break;
-            const int q = u / D.n_strips;
-            const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
-            next = n;
-            if (!units::run_unit<NS, INV, true>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp,
-                                                &next))
-                break;
-            units::order_done(D, seg, lane);
+        // ordered in-place launch: tickets in segment order, one per group of
+        // kWarpsPerCta consecutive units (adjacent strips of a segment, as a
+        // CTA of the plain launch holds them); a unit waits (after issuing its
+        // first loads, before its first store) only for units of earlier
+        // tickets, which are running.  Warp 0 takes the next ticket a few
+        // stages before the end of its unit.
+        __shared__ int s_group[2];
+        if (threadIdx.x == 0) s_group[0] = atomicAdd(D.order, 1);
+        __syncthreads();
+        bool alive = true;
+        for (int k = 0;; k ^= 1) {
+            const int g = s_group[k];
+            if (g >= ceil_div(n, kWarpsPerCta)) break;  // the same for the whole CTA
+            const int u = g * kWarpsPerCta + warp;
+            int next = warp == 0 ? -1 : 0;
+            if (alive && u < n) {
+                const int q = u / D.n_strips;
+                const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
+                alive = units::run_unit<NS, INV, true>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch,
+                                                       mp, next);
+                if (alive) units::order_done(D, seg, lane);
+            }
+            if (warp == 0 && lane == 0) s_group[k ^ 1] = next >= 0 ? next : atomicAdd(D.order, 1);
+            __syncthreads();
         }
     } else {
         for (int u = blockIdx.x * kWarpsPerCta + warp; u < n; u += gridDim.x * kWarpsPerCta) {
             const int q = u / D.n_strips;
             const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
-            if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp))
+            int unused = 0;
+            if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp, unused))
                 break;
         }
     }

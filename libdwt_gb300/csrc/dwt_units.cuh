@@ -305,7 +305,7 @@ struct WarpPipe {
 // frame is done.  order_done: counts a
 // finished strip of `seg`; every read of the unit has completed (its stages
 // were waited for), which is all a later writer of those rows needs.
-// order_ticket: lane 0 takes the warp's next ticket.
+// order_ticket: lane 0 takes the next ticket, when `next` is armed (< 0).
 constexpr uint32_t kOrderWaitLimit = 1u << 24;
 
 __device__ __forceinline__ bool order_wait(const LevelDesc &D, bool inverse, int lat, int seg, int lane, int *err,
@@ -343,9 +343,9 @@ __device__ __forceinline__ void order_done(const LevelDesc &D, int seg, int lane
     if (lane == 0) atomicAdd(D.order + 1 + seg, 1);
 }
 
-__device__ __forceinline__ void order_ticket(const LevelDesc &D, int lane, int *next)
+__device__ __forceinline__ void order_ticket(const LevelDesc &D, int lane, int &next)
 {
-    if (lane == 0) *next = atomicAdd(D.order, 1);
+    if (lane == 0 && next < 0) next = atomicAdd(D.order, 1);  // armed by a negative value
 }
 
 // Waits (bounded) for the first `count` stages a unit has issued, so that
@@ -379,7 +379,7 @@ __device__ __forceinline__ void unit_span(const LevelDesc &D, int seg, int &k0, 
 // on, `win` columns wide, `slot_f` floats per row slot.
 template <int NS, bool EDGE, class Pipe, bool ORD = false>
 __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
-                             int win, int slot_f, uint32_t &tick, int lane, int *err, int *next = nullptr)
+                             int win, int slot_f, uint32_t &tick, int lane, int *err, int &next)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
@@ -686,7 +686,7 @@ __device__ __forceinline__ void v_inverse2(f2 A, f2 B, f2 &o, f2 &e1, f2 &o1, f2
 template <int NS, bool EDGE, class Pipe, bool ORD = false>
 __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
                              int band_win, const LevelMaps *maps, uint32_t &tick, int lane, int *err,
-                             int *next = nullptr)
+                             int &next)
 {
     constexpr int LAT = NS / 2;
     const int w = D.w, h = D.h;
@@ -905,7 +905,7 @@ __device__ __forceinline__ bool fast_ok(const LevelDesc &D)
 template <int NS, bool INV, bool ORD = false>
 __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
                                          uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch,
-                                         const LevelMaps *maps = nullptr, int *next = nullptr)
+                                         const LevelMaps *maps, int &next)
 {
     if (D.h == 1 || D.rows_only)
         return INV ? inverse_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err)
