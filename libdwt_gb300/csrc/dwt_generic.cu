@@ -8,6 +8,7 @@
 //     in between untouched (src/libdwt.c:6354-6375), then optional zero
 //     padding (src/libdwt.c:6377-6397, 6729-6745).
 #include "dwt_generic.cuh"
+#include "dwt_recur.cuh"
 
 #include <algorithm>
 #include <cstdint>
@@ -209,57 +210,75 @@ __global__ void zero_inverse_kernel(float *base, long long ls, long long es, int
     for (int i = N; i < n_dst; ++i) line[i * es] = 0.0f;
 }
 
-// The per-line levels of a sparse frame in one CTA: the level frame of the
-// first of them (ox0 x oy0 samples of f, pitch in floats) is brought into
-// shared memory, every level runs the reference's sequence there (row pass
-// over the outer rows, column pass over the outer columns, zero padding;
-// inverse: the same with the inverse line transform), separated by block
-// barriers, and the frame goes back.  Forward levels j0 .. j1-1, inverse
-// levels j1 .. j0+1 (j0 < j1), sizes by ceil_div_pow2 of the outer and inner
-// sizes of level 0.
-template <bool INV>
-__global__ void __launch_bounds__(512) sparse_tail_kernel(float *f, long long pitch, int ox, int oy, int ix, int iy,
-                                                          int j0, int j1, const Wavelet W)
+// The small levels of a zero-padded sparse frame in one CTA: the level
+// frame of the first of them (fx x fy samples of f, pitch in floats) is
+// brought into shared memory and every level runs there as the dense inner
+// level with its H bands at the outer midpoints -- a row pass over the inner
+// rows, a column pass over the L and H columns, both as per-thread lifting
+// windows (dwt_recur.cuh) -- followed by zeros over the rest of the level's
+// frame, which is what the reference's per-line sequence with zero padding
+// leaves there (src/libdwt.c:6353-6397, 6700-6745; the samples it computes
+// outside the inner bands are overwritten or zeroed).  Forward levels j0 ..
+// j1-1, inverse levels j1 .. j0+1 (j0 < j1), sizes by ceil_div_pow2 of the
+// outer and inner sizes of level 0.
+constexpr int kTailThreads = 512;
+// windows of 2 output pairs, as in the coarse kernel: these levels are
+// latency-bound and short per-thread chains win
+constexpr int kTailWindowPairs = 2;
+
+template <int NS, bool INV>
+__global__ void __launch_bounds__(kTailThreads) sparse_tail_kernel(float *f, long long pitch, int ox, int oy, int ix,
+                                                                   int iy, int j0, int j1, const Wavelet W)
 {
     extern __shared__ float sh[];
     const int fx = ceil_div_pow2(ox, j0), fy = ceil_div_pow2(oy, j0);
     const int ps = fx | 1;  // odd pitch: the lines of a column pass fall in different banks
     float *S = sh, *T = sh + ps * fy;
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int k = tid; k < fx * fy; k += nt) S[(k / fx) * ps + k % fx] = f[(long long)(k / fx) * pitch + k % fx];
+    recur::for_rect(0, fx, 0, fy, tid, nt, [&](int x, int y) { S[y * ps + x] = f[(long long)y * pitch + x]; });
     __syncthreads();
+    // zeros over [0, w) x [0, h) of S outside the rectangles [x0, x1) x [y0, y1) of `keep`
+    auto zero_outside = [&](int w, int h, const int (*keep)[4], int nk) {
+        recur::for_rect(0, w, 0, h, tid, nt, [&](int x, int y) {
+            for (int k = 0; k < nk; ++k)
+                if (x >= keep[k][0] && x < keep[k][1] && y >= keep[k][2] && y < keep[k][3]) return;
+            S[y * ps + x] = 0.0f;
+        });
+    };
     for (int step = 0; step < j1 - j0; ++step) {
         if (!INV) {
             const int j = j0 + step;
             const int osx = ceil_div_pow2(ox, j), osy = ceil_div_pow2(oy, j);
             const int odx = ceil_div_pow2(ox, j + 1), ody = ceil_div_pow2(oy, j + 1);
             const int isx = ceil_div_pow2(ix, j), isy = ceil_div_pow2(iy, j);
-            for (int k = tid; k < osy; k += nt) line_forward_one(S + k * ps, 1, isx, odx, T + k, osy, W);
+            const int lx = (isx + 1) / 2, hx = isx / 2, ly = (isy + 1) / 2, hy = isy / 2;
+            recur::pass<NS, false, kTailWindowPairs>(S, ps, 1, T, ps, 1, isy, isx, W, tid, nt, odx);  // inner rows
             __syncthreads();
-            for (int k = tid; k < osx; k += nt) line_forward_one(S + k, ps, isy, ody, T + k, osx, W);
+            recur::pass<NS, false, kTailWindowPairs>(T, 1, ps, S, 1, ps, lx, isy, W, tid, nt, ody);  // L columns
+            recur::pass<NS, false, kTailWindowPairs>(T + odx, 1, ps, S + odx, 1, ps, hx, isy, W, tid, nt, ody);  // H columns
             __syncthreads();
-            for (int k = tid; k < osy; k += nt) zero_forward_one(S + k * ps, 1, isx, odx, osx - odx, odx);
-            __syncthreads();
-            for (int k = tid; k < osx; k += nt) zero_forward_one(S + k, ps, isy, ody, osy - ody, ody);
+            const int keep[4][4] = {{0, lx, 0, ly}, {odx, odx + hx, 0, ly}, {0, lx, ody, ody + hy},
+                                    {odx, odx + hx, ody, ody + hy}};
+            zero_outside(osx, osy, keep, 4);
             __syncthreads();
         } else {
             const int j = j1 - step;  // LL_j -> LL_{j-1}
             const int osx = ceil_div_pow2(ox, j), osy = ceil_div_pow2(oy, j);
             const int odx = ceil_div_pow2(ox, j - 1), ody = ceil_div_pow2(oy, j - 1);
             const int idx = ceil_div_pow2(ix, j - 1), idy = ceil_div_pow2(iy, j - 1);
-            for (int k = tid; k < ody; k += nt) line_inverse_one(S + k * ps, 1, idx, osx, T + k, ody, W);
+            const int ly = (idy + 1) / 2, hy = idy / 2;
+            // rows holding bands (L rows at the top, H rows from the outer midpoint)
+            recur::pass<NS, true, kTailWindowPairs>(S, ps, 1, T, ps, 1, ly, idx, W, tid, nt, osx);
+            recur::pass<NS, true, kTailWindowPairs>(S + osy * ps, ps, 1, T + osy * ps, ps, 1, hy, idx, W, tid, nt, osx);
             __syncthreads();
-            for (int k = tid; k < odx; k += nt) line_inverse_one(S + k, ps, idy, osy, T + k, odx, W);
+            recur::pass<NS, true, kTailWindowPairs>(T, 1, ps, S, 1, ps, idx, idy, W, tid, nt, osy);
             __syncthreads();
-            for (int k = tid; k < ody; k += nt)
-                for (int i = idx; i < odx; ++i) S[k * ps + i] = 0.0f;
-            __syncthreads();
-            for (int k = tid; k < odx; k += nt)
-                for (int i = idy; i < ody; ++i) S[i * ps + k] = 0.0f;
+            const int keep[1][4] = {{0, idx, 0, idy}};
+            zero_outside(odx, ody, keep, 1);
             __syncthreads();
         }
     }
-    for (int k = tid; k < fx * fy; k += nt) f[(long long)(k / fx) * pitch + k % fx] = S[(k / fx) * ps + k % fx];
+    recur::for_rect(0, fx, 0, fy, tid, nt, [&](int x, int y) { f[(long long)y * pitch + x] = S[y * ps + x]; });
 }
 
 // Zero fill of a list of rectangles of a frame (pitch in floats): blocks take
@@ -596,7 +615,7 @@ cudaError_t launch_scatter_calls(const CallRow *calls, int n_calls, int N, bool 
 size_t sparse_tail_smem(int ox, int oy, int j0)
 {
     const int fx = ceil_div_pow2(ox, j0), fy = ceil_div_pow2(oy, j0);
-    return size_t(fx | 1) * fy * 4 + size_t(fx) * fy * 4;
+    return size_t(fx | 1) * fy * 4 * 2;
 }
 
 cudaError_t launch_sparse_tail(bool inverse, float *f, long long pitch, int ox, int oy, int ix, int iy, int j0,
@@ -604,17 +623,28 @@ cudaError_t launch_sparse_tail(bool inverse, float *f, long long pitch, int ox, 
 {
     const size_t smem = sparse_tail_smem(ox, oy, j0);
     if (smem > kSparseTailSmem || j1 <= j0) return cudaErrorInvalidValue;
-    static const cudaError_t cf = cudaFuncSetAttribute(sparse_tail_kernel<false>,
-                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSparseTailSmem);
-    static const cudaError_t ci = cudaFuncSetAttribute(sparse_tail_kernel<true>,
-                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, kSparseTailSmem);
-    if (cf != cudaSuccess) return cf;
-    if (ci != cudaSuccess) return ci;
+    static const cudaError_t configured = [] {
+        cudaError_t e = cudaSuccess;
+        for (auto k : {sparse_tail_kernel<4, false>, sparse_tail_kernel<4, true>, sparse_tail_kernel<2, false>,
+                       sparse_tail_kernel<2, true>})
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSparseTailSmem);
+        return e;
+    }();
+    if (configured != cudaSuccess) return configured;
     const Wavelet W = make_wavelet(wavelet, inverse);
-    if (inverse)
-        sparse_tail_kernel<true><<<1, 512, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
-    else
-        sparse_tail_kernel<false><<<1, 512, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+    const dim3 g(1), b(kTailThreads);
+    if (wavelet == CDF97) {
+        if (inverse)
+            sparse_tail_kernel<4, true><<<g, b, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+        else
+            sparse_tail_kernel<4, false><<<g, b, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+    } else {
+        if (inverse)
+            sparse_tail_kernel<2, true><<<g, b, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+        else
+            sparse_tail_kernel<2, false><<<g, b, smem, s>>>(f, pitch, ox, oy, ix, iy, j0, j1, W);
+    }
     return cudaGetLastError();
 }
 

@@ -182,9 +182,11 @@ __device__ __forceinline__ int reflect(int r, int n)
     return r;
 }
 
+// hoff: sample index of H_0 in y (ceil(n/2) in the reference layout; the
+// outer midpoint in a zero-padded sparse frame).
 template <int NS, int SEG>
 __device__ __forceinline__ void window_forward(const float *x, int xs, int n, float *y, int ys, int k0,
-                                               const Wavelet &W)
+                                               const Wavelet &W, int hoff)
 {
     constexpr int WN = 2 * SEG + 2 * NS;
     const int s0 = 2 * k0 - NS;  // even: window index parity = sample parity
@@ -212,7 +214,7 @@ __device__ __forceinline__ void window_forward(const float *x, int xs, int n, fl
         const int p = k0 + j;
         if (p < nl) {
             y[p * ys] = fmul(v[NS + 2 * j], W.zeta_e);
-            if (2 * p + 1 < n) y[(nl + p) * ys] = fmul(v[NS + 2 * j + 1], W.zeta_o);
+            if (2 * p + 1 < n) y[(hoff + p) * ys] = fmul(v[NS + 2 * j + 1], W.zeta_o);
         }
     }
 }
@@ -222,10 +224,10 @@ __device__ __forceinline__ void window_forward(const float *x, int xs, int n, fl
 // run in the inverse order (even samples first).
 template <int NS, int SEG>
 __device__ __forceinline__ void window_inverse(const float *x, int xs, int n, float *y, int ys, int k0,
-                                               const Wavelet &W)
+                                               const Wavelet &W, int hoff)
 {
     constexpr int WN = 2 * SEG + 2 * NS;
-    const int nl = (n + 1) >> 1;
+    const int nl = hoff;  // H_j at x[(hoff + j) * xs]
     const int s0 = 2 * k0 - NS;
     float v[WN];
     if (s0 >= 0 && s0 + WN <= n) {
@@ -260,15 +262,17 @@ __device__ __forceinline__ void window_inverse(const float *x, int xs, int n, fl
 }
 
 // One pass over `nl` lines of length n, line l at src + l*ls (sample stride
-// xs) into dst + l*ds (stride ys), by threads tid of nthreads, one window
+// xs) into dst + l*ds (stride ys), H at sample hoff (ceil(n/2) by default),
+// by threads tid of nthreads, one window
 // (line, segment of SEG output pairs) per item; consecutive threads take
 // consecutive lines.  Long windows do less halo work, short ones have
 // shorter dependency chains per thread.  A line of length 1 is only scaled
 // (the reference's one-sample transform).
 template <int NS, bool INV, int SEG = kSegPairs>
 __device__ __forceinline__ void pass(const float *src, int ls, int xs, float *dst, int ds, int ys, int nl, int n,
-                                     const Wavelet &W, int tid, int nthreads)
+                                     const Wavelet &W, int tid, int nthreads, int hoff = -1)
 {
+    if (hoff < 0) hoff = (n + 1) >> 1;
     if (n == 1) {
         const float z = INV ? W.n1_inv : W.n1_fwd;
         for (int l = tid; l < nl; l += nthreads) dst[l * ds] = fmul(src[l * ls], z);
@@ -279,9 +283,9 @@ __device__ __forceinline__ void pass(const float *src, int ls, int xs, float *ds
     for (int t = tid; t < items; t += nthreads) {
         const int sgi = t / nl, l = t - sgi * nl;
         if (INV)
-            window_inverse<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W);
+            window_inverse<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W, hoff);
         else
-            window_forward<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W);
+            window_forward<NS, SEG>(src + l * ls, xs, n, dst + l * ds, ys, sgi * SEG, W, hoff);
     }
 }
 
