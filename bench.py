@@ -849,6 +849,30 @@ def run_signals_extra(D, torch, checks: dict, groups=8192, n=4097, lanes=8):
             "c4_inv_frac_alg": round(8 * samples / ti / 1e9 / peak, 4), **percall}
 
 
+def native_calls_1d():
+    """The OpenMP driver of the per-signal calls (libdwt_gb300/harness/calls_1d.c),
+    built against the library on first use; None when it cannot be built."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from libdwt_gb300.buildext import LIB
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libdwt_gb300", "harness", "calls_1d.c")
+    out = os.path.join(os.path.dirname(LIB), "libcalls_1d.so")
+    cc = shutil.which("gcc")
+    if not cc or not os.path.exists(src):
+        return None
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        r = subprocess.run([cc, "-O2", "-fopenmp", "-shared", "-fPIC", src, "-o", out, "-L", os.path.dirname(LIB),
+                            "-l:" + os.path.basename(LIB), "-Wl,-rpath," + os.path.dirname(LIB)],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            return None
+    lib = C.CDLL(out)
+    lib.calls_1d.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int]
+    lib.calls_1d.restype = C.c_double
+    return lib
+
+
 def c4_per_call(D, torch, bank, n, lanes, n_groups=512, threads=16):
     """The reference's own calling pattern for the signal bank, against this
     library: `threads` host threads, each calling the drop-in
@@ -886,6 +910,15 @@ def c4_per_call(D, torch, bank, n, lanes, n_groups=512, threads=16):
         out[f"c4_dropin_per_call_{where}_us"] = round(dt / count * threads * 1e6, 1)
     out["c4_dropin_per_call_sample"] = (f"{count} signals of {n} (the first {n_groups} groups), {threads} host "
                                         f"threads, one dwt_cdf97_f_ex_stride_s call per signal")
+    # the same calls from native code: an OpenMP loop, as the reference's callers run it
+    nat = native_calls_1d()
+    if nat is not None:
+        for where, base in (("host", part.ctypes.data), ("device", dev.data_ptr())):
+            nat.calls_1d(0, base, n, st, lanes, gs, lanes, threads)  # warm-up
+            torch.cuda.synchronize()
+            dt = nat.calls_1d(0, base, n, st, lanes, gs, count, threads)
+            out[f"c4_dropin_per_call_openmp_{where}_gsamples_s"] = round(count * n / dt / 1e9, 4)
+            out[f"c4_dropin_per_call_openmp_{where}_us"] = round(dt / count * threads * 1e6, 1)
     return out
 
 

@@ -11,6 +11,7 @@
 //      straight into a dense device caller frame).
 // Out of place is what makes the fused kernel legal: the reference works in
 // place, where one tile's outputs land on other tiles' inputs.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,6 +21,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -84,6 +86,10 @@ Context &ctx()
             cudaStreamCreateWithPriority(&l.s_out, cudaStreamNonBlocking, greatest);
             cudaMalloc(&l.d_err, sizeof(int));
             cudaMemset(l.d_err, 0, sizeof(int));
+            if (cudaHostAlloc(reinterpret_cast<void **>(&l.h_err), sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+                l.h_err = nullptr;
+                cudaGetLastError();
+            }
         }
         cudaDeviceSynchronize();
         g_ctx = c;
@@ -109,6 +115,8 @@ void ctx_finish()
         cudaStreamDestroy(l.s_out);
         cudaStreamDestroy(l.stream);
         cudaFree(l.d_err);
+        if (l.h_err) cudaFreeHost(l.h_err);
+        l.h_err = nullptr;
     }
     cudaStreamDestroy(g_ctx->stream);
     delete g_ctx;
@@ -196,6 +204,35 @@ static int check_device_error(int *d_err)
 }
 static int check_device_error(Context &c) { return check_device_error(c.d_err); }
 static int check_device_error(Lane &l) { return check_device_error(l.d_err); }
+
+// The end of a call on a lane: waits for the lane's stream and reports (and
+// clears) its device error word, which the same stream copies into pinned
+// host memory first, so that one synchronisation serves both (a separate
+// synchronous copy of the word cost about as much as a small call's work).
+static int lane_finish(Lane &l)
+{
+    if (!l.h_err) {
+        if (cudaStreamSynchronize(l.stream) != cudaSuccess) {
+            log_error("CUDA error %s\n", cudaGetErrorString(cudaGetLastError()));
+            return DWT_GPU_ECUDA;
+        }
+        return check_device_error(l);
+    }
+    cudaError_t e = cudaMemcpyAsync(l.h_err, l.d_err, sizeof(int), cudaMemcpyDeviceToHost, l.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(l.stream);
+    if (e != cudaSuccess) {
+        log_error("CUDA error %s\n", cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? DWT_GPU_ENOMEM : DWT_GPU_ECUDA;
+    }
+    const int h = *reinterpret_cast<volatile int *>(l.h_err);
+    if (h) {
+        cudaMemsetAsync(l.d_err, 0, sizeof(int), l.stream);
+        cudaStreamSynchronize(l.stream);
+        log_error("device-side wait gave up (code %d)\n", h);
+        return DWT_GPU_EDEVICE;
+    }
+    return DWT_GPU_OK;
+}
 
 // ------------------------------------------------------- level pipelines
 
@@ -632,8 +669,7 @@ static int pipelined_forward(Lane &c, int wavelet, char *host, long long sx, int
     int evo = 0;
     CK(R.record(so, evo));
     CK(cudaStreamWaitEvent(s, c.event(evo), 0));
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 static int pipelined_inverse(Lane &c, int wavelet, char *host, long long sx, int W, int H, int J, bool direct)
@@ -707,8 +743,7 @@ static int pipelined_inverse(Lane &c, int wavelet, char *host, long long sx, int
     cudaEvent_t eo = record(so);
     if (!eo) return set_error(DWT_GPU_ECUDA);
     CK(cudaStreamWaitEvent(s, eo, 0));
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // ------------------------------------------------ in place on device frames
@@ -891,8 +926,7 @@ static int inplace_device(Lane &c, int wavelet, bool inverse, float *F, long lon
         CK(cudaStreamWaitEvent(s, e_copy, 0));
         CK(launch_level(d0, wavelet, true, s, c.d_err));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // ----------------------------------------- sparse frames with zero padding
@@ -1284,8 +1318,7 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
         sparse_fast_ok(ptr, csx / 4, ox, oy, ix, iy, J)) {
         const int rc = sparse_inplace(c, wavelet, inverse, static_cast<float *>(ptr), csx / 4, ox, oy, ix, iy, J);
         if (rc != DWT_GPU_OK) return rc;
-        CK(cudaStreamSynchronize(s));
-        return set_error(check_device_error(c));
+        return set_error(lane_finish(c));
     }
 
     // 1. stage into IN
@@ -1383,8 +1416,7 @@ static int run_2d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox, 
     } else if (!direct) {
         CK(launch_unpack(out, out_pitch, ptr, sx, sy, ox, oy, s));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // ------------------------------------------------------------ 1D driver
@@ -1451,8 +1483,7 @@ static int run_2d_d(int wavelet, bool inverse, void *ptr, int sx, int sy, int ox
     } else {
         CK(launch_unpack_d(f, P, ptr, sx, sy, ox, oy, s));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // The double-precision strided 1D level (libdwt's _ex_stride_d): the samples
@@ -1504,8 +1535,7 @@ static int run_1d_d(int wavelet, bool inverse, const double *a, const double *b,
         CK(line_d(true, x, N, wavelet, static_cast<double *>(tmp.p), s));
         CK(scatter(x, c_l, N));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // ------------------------------------------- strided 1D: combined calls
@@ -1514,12 +1544,13 @@ static int run_1d_d(int wavelet, bool inverse, const double *a, const double *b,
 // dwt_cdf97_f_ex_stride_s call per signal, often from several OpenMP threads
 // at once (src/libdwt.c:5512-5557).  One call costs a few launches and a
 // synchronisation, tens of microseconds, almost all of it fixed cost; so
-// calls that arrive while another thread's batch is on the GPU are combined:
-// the thread that finds no batch running takes every pending call, gathers
-// their samples into the rows of one frame, transforms all rows in one
-// launch per (wavelet, direction, length) and scatters the results, and the
-// calls it took return once that has synchronised.  A thread calling alone
-// gets a batch of one.  Only calls whose memory the kernels address
+// calls that arrive while other threads' batches are on the GPU are
+// combined: a thread that finds fewer than combine_batches() batches running
+// takes every pending call, gathers their samples into the rows of one frame
+// (the rows' addresses travel as kernel parameters), transforms all rows in
+// one launch per (wavelet, direction, length) and scatters the results, and
+// the calls it took return once that has synchronised.  A thread calling
+// alone gets a batch of one.  Only calls whose memory the kernels address
 // directly are combined (device and managed memory, and pageable host memory
 // where the GPU walks the host's page tables); the others take the per-call
 // path below.  DWT_GPU_COMBINE_1D=0 turns combining off.
@@ -1535,7 +1566,20 @@ struct PendingCall {
 static std::mutex g_comb_mu;
 static std::condition_variable g_comb_cv;
 static std::vector<PendingCall *> g_comb_pending;
-static bool g_comb_running = false;
+static int g_comb_running = 0;  // batches in flight
+
+// Batches in flight at once, each on its own lane (2; DWT_GPU_COMBINE_BATCHES,
+// 1 .. 8): a thread whose call arrives while the limit is reached waits for
+// one to finish, then takes every queued call.
+static int combine_batches()
+{
+    static const int n = [] {
+        const char *e = getenv("DWT_GPU_COMBINE_BATCHES");
+        const int v = e ? atoi(e) : 0;
+        return v >= 1 && v <= 8 ? v : 2;
+    }();
+    return n;
+}
 
 static bool combine_enabled()
 {
@@ -1546,10 +1590,60 @@ static bool combine_enabled()
     return on;
 }
 
-static bool kernel_reaches(const void *p)
+// The kind of p and, for CUDA allocations (device, managed, pinned), the
+// allocation holding it, [lo, hi): one driver query, so that the other
+// pointers of a call that fall in the same allocation need none.  Memory the
+// driver does not know is pageable host memory (as classify has it).
+static MemKind classify_range(const void *p, uintptr_t &lo, uintptr_t &hi)
 {
-    const MemKind k = classify(p);
+    using Fn = CUresult (*)(unsigned int, CUpointer_attribute *, void **, CUdeviceptr);
+    static const Fn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<Fn>(f);
+    }();
+    lo = hi = 0;
+    if (!fn) return classify(p);
+    unsigned int type = 0;
+    int managed = 0;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    CUpointer_attribute attrs[4] = {CU_POINTER_ATTRIBUTE_MEMORY_TYPE, CU_POINTER_ATTRIBUTE_IS_MANAGED,
+                                    CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, CU_POINTER_ATTRIBUTE_RANGE_SIZE};
+    void *vals[4] = {&type, &managed, &start, &size};
+    if (fn(4, attrs, vals, reinterpret_cast<CUdeviceptr>(p)) != CUDA_SUCCESS || type == 0) return MemKind::Pageable;
+    if (size > 0) {
+        lo = uintptr_t(start);
+        hi = lo + size;
+    }
+    if (managed || type == CU_MEMORYTYPE_UNIFIED) return MemKind::Managed;
+    return type == CU_MEMORYTYPE_DEVICE ? MemKind::Device : MemKind::Pinned;
+}
+
+static bool reaches(MemKind k)
+{
     return k == MemKind::Device || k == MemKind::Managed || (k == MemKind::Pageable && pageable_direct());
+}
+
+// Whether the kernels address every given pointer (nulls and repeats
+// skipped), with one driver query per distinct CUDA allocation.
+static bool kernel_reaches_all(const void *first, std::initializer_list<const void *> others)
+{
+    uintptr_t lo = 0, hi = 0;
+    if (!reaches(classify_range(first, lo, hi))) return false;
+    for (const void *q : others) {
+        if (!q || q == first) continue;
+        const uintptr_t u = reinterpret_cast<uintptr_t>(q);
+        if (u >= lo && u < hi) continue;
+        uintptr_t l2, h2;
+        if (!reaches(classify_range(q, l2, h2))) return false;
+    }
+    return true;
 }
 
 // One (wavelet, direction, length) group of combined calls: gather, one
@@ -1565,11 +1659,22 @@ static int run_1d_rows(int wavelet, bool inverse, int N, PendingCall *const *cal
     const long long P = align_up(N + 4, 32);
     std::vector<CallRow> rows(n);
     for (int k = 0; k < n; ++k) rows[k] = calls[k]->row;
-    Buf desc(sizeof(CallRow) * n + 256, s), in(size_t(P) * n * 4 + 256, s), out(size_t(P) * n * 4 + 256, s);
-    if (!desc.p || !in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
-    CK(cudaMemcpyAsync(desc.p, rows.data(), sizeof(CallRow) * n, cudaMemcpyHostToDevice, s));
-    const CallRow *d_rows = static_cast<const CallRow *>(desc.p);
-    CK(launch_gather_calls(d_rows, n, N, inverse, in.f(), P, nl4, s));
+    // up to kCallRowsParam rows travel as kernel parameters, more as a device array
+    Buf desc;
+    const CallRow *d_rows = nullptr;
+    if (n > kCallRowsParam) {
+        if (!desc.alloc(sizeof(CallRow) * n + 256, s)) return set_error(DWT_GPU_ENOMEM);
+        CK(cudaMemcpyAsync(desc.p, rows.data(), sizeof(CallRow) * n, cudaMemcpyHostToDevice, s));
+        d_rows = static_cast<const CallRow *>(desc.p);
+    }
+    if (N <= kCalls1dMaxN) {
+        // one launch: gather, lift and scatter per call in shared memory
+        CK(launch_calls_1d(d_rows, rows.data(), n, N, wavelet, inverse, s));
+        return set_error(lane_finish(c));
+    }
+    Buf in(size_t(P) * n * 4 + 256, s), out(size_t(P) * n * 4 + 256, s);
+    if (!in.p || !out.p) return set_error(DWT_GPU_ENOMEM);
+    CK(launch_gather_calls(d_rows, rows.data(), n, N, inverse, in.f(), P, nl4, s));
     LevelDesc d{};
     d.w = N;
     d.h = n;
@@ -1588,9 +1693,8 @@ static int run_1d_rows(int wavelet, bool inverse, int N, PendingCall *const *cal
     }
     plan_level(d, 0, inverse);
     CK(launch_level(d, wavelet, inverse, s, c.d_err));
-    CK(launch_scatter_calls(d_rows, n, N, inverse, out.f(), P, s));
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    CK(launch_scatter_calls(d_rows, rows.data(), n, N, inverse, out.f(), P, s));
+    return set_error(lane_finish(c));
 }
 
 static void run_combined(std::vector<PendingCall *> &batch)
@@ -1618,15 +1722,15 @@ static int run_1d_combined(PendingCall &me)
     std::unique_lock<std::mutex> lk(g_comb_mu);
     g_comb_pending.push_back(&me);
     while (!me.done) {
-        if (!g_comb_running) {
-            g_comb_running = true;
+        if (g_comb_running < combine_batches() && !g_comb_pending.empty()) {
+            ++g_comb_running;
             std::vector<PendingCall *> batch;
             batch.swap(g_comb_pending);
             lk.unlock();
             run_combined(batch);
             lk.lock();
             for (PendingCall *q : batch) q->done = true;
-            g_comb_running = false;
+            --g_comb_running;
             g_comb_cv.notify_all();
         } else {
             g_comb_cv.wait(lk);
@@ -1654,9 +1758,8 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
     }
     if (combine_enabled()) {
         const int nh = N / 2;
-        const bool reach = kernel_reaches(a) && kernel_reaches(c_l) &&
-                           (!inverse || nh == 0 || (b && kernel_reaches(b))) &&
-                           (inverse || nh == 0 || (h_out && kernel_reaches(h_out)));
+        const bool reach = (!inverse || nh == 0 || b) && (inverse || nh == 0 || h_out) &&
+                           kernel_reaches_all(a, {c_l, inverse && nh ? b : nullptr, !inverse && nh ? h_out : nullptr});
         if (reach) {
             PendingCall me{wavelet, inverse, N, CallRow{a, b, c_l, h_out, stride}, DWT_GPU_OK, false};
             return set_error(run_1d_combined(me));
@@ -1720,8 +1823,7 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
     } else {
         CK(scatter(out.f(), c_l, N));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // Batched strided 1D, in place: gather every signal into a row of IN,
@@ -1763,8 +1865,7 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
         if (!on_device)
             CK(cudaMemcpyAsync(base, span.p, size_t((groups - 1) * group_stride + 4LL * N * group),
                                cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        return set_error(check_device_error(c));
+        return set_error(lane_finish(c));
     }
 
     const long long P = align_up(N + 4, 32);
@@ -1805,8 +1906,7 @@ int run_1d_batch(int wavelet, bool inverse, void *base, int N, int stride, long 
     void *dst = on_device ? base : span.p;
     CK(launch_scatter_signals(out.f(), P, N, dst, stride, count, group, group_stride, lane_stride, s));
     if (!on_device) CK(cudaMemcpyAsync(base, span.p, size_t(sb), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 // Every channel of a dense interleaved float image in one call: one copy of
@@ -1870,8 +1970,7 @@ static int run_2d_channels(int wavelet, bool inverse, void *ptr, int stride_x, i
     } else {
         CK(launch_interleave(out.f(), P, plane, channels, w, h, ptr, stride_x, s));
     }
-    CK(cudaStreamSynchronize(s));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 int run_2d_dev(int wavelet, bool inverse, const float *src, long long src_pitch_bytes, float *dst,
@@ -2086,8 +2185,7 @@ int dwt_gpu_selftest_wait_timeout(int iterations)
     Lane &c = lane_guard.get();
     wait_timeout_kernel<<<1, 32, 0, c.stream>>>(uint32_t(iterations), c.d_err);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(c.stream));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 int dwt_gpu_selftest_inplace_wait_timeout(int iterations)
@@ -2101,8 +2199,7 @@ int dwt_gpu_selftest_inplace_wait_timeout(int iterations)
     if (!order.p) return set_error(DWT_GPU_ENOMEM);
     CK(cudaMemsetAsync(order.p, 0, bytes, c.stream));
     CK(launch_order_wait_timeout(uint32_t(iterations), static_cast<int *>(order.p), c.d_err, c.stream));
-    CK(cudaStreamSynchronize(c.stream));
-    return set_error(check_device_error(c));
+    return set_error(lane_finish(c));
 }
 
 int dwt_gpu_inplace_plan(int wavelet, int inverse, int w, int h, int detail_row, int *seg_pairs, int *n_segs,

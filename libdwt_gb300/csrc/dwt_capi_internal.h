@@ -25,6 +25,7 @@ struct Lane {
     cudaStream_t s_in = nullptr, s_out = nullptr;  // copies of the pipelined host path
     std::vector<cudaEvent_t> events;                 // copy and band events of the pipelined host path
     int *d_err = nullptr;
+    int *h_err = nullptr;  // pinned host copy of d_err, read after the stream's synchronisation
 
     // Event i of the lane (created on first use; timing disabled).  The
     // caller holds mu.

@@ -305,12 +305,12 @@ __global__ void zero_rects_kernel(float *f, long long pitch, const ZeroRects R)
 // (forward: N samples; inverse: ceil(N/2) of L at a[k] into [0, ..) and
 // floor(N/2) of H at b[k] into [h_off, ..)); results go to c[k] (forward: L
 // and then H to h[k]; inverse: N samples), same strides.
-__global__ void gather_calls_kernel(const CallRow *calls, int n_calls, int N, bool inverse, float *dst,
-                                    long long dpitch, int h_off)
+__global__ void gather_calls_kernel(const CallRow *calls, const __grid_constant__ CallRowsParam P, int n_calls, int N,
+                                    bool inverse, float *dst, long long dpitch, int h_off)
 {
     const int k = blockIdx.y;
     if (k >= n_calls) return;
-    const CallRow r = calls[k];
+    const CallRow r = calls ? calls[k] : P.r[k];
     float *row = dst + (long long)k * dpitch;
     const int nl = (N + 1) / 2;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
@@ -321,12 +321,12 @@ __global__ void gather_calls_kernel(const CallRow *calls, int n_calls, int N, bo
     }
 }
 
-__global__ void scatter_calls_kernel(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
-                                     long long spitch)
+__global__ void scatter_calls_kernel(const CallRow *calls, const __grid_constant__ CallRowsParam P, int n_calls, int N,
+                                     bool inverse, const float *src, long long spitch)
 {
     const int k = blockIdx.y;
     if (k >= n_calls) return;
-    const CallRow r = calls[k];
+    const CallRow r = calls ? calls[k] : P.r[k];
     const float *row = src + (long long)k * spitch;
     const int nl = (N + 1) / 2;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
@@ -334,6 +334,40 @@ __global__ void scatter_calls_kernel(const CallRow *calls, int n_calls, int N, b
             store_any(static_cast<unsigned char *>(r.c) + (long long)i * r.stride, row[i]);
         else
             store_any(static_cast<unsigned char *>(r.h) + (long long)(i - nl) * r.stride, row[i]);
+    }
+}
+
+// Combined strided 1D calls in one launch, one block per call: the call's
+// samples (forward: N at a; inverse: L at a, H at b) are gathered into
+// shared memory, lifted there as per-thread windows of one line
+// (dwt_recur.cuh), and stored back at the call's destinations (forward: L
+// at c, H at h; inverse: N samples at c), all `stride` bytes apart.
+constexpr int kCalls1dThreads = 256;
+
+template <int NS, bool INV>
+__global__ void __launch_bounds__(kCalls1dThreads) calls_1d_kernel(const CallRow *calls,
+                                                                   const __grid_constant__ CallRowsParam P,
+                                                                   int n_calls, int N, const Wavelet W)
+{
+    extern __shared__ float sm1[];
+    const int k = blockIdx.x;
+    if (k >= n_calls) return;
+    const CallRow r = calls ? calls[k] : P.r[k];
+    float *A = sm1, *B = sm1 + N;
+    const int nl = (N + 1) / 2, tid = threadIdx.x, nt = blockDim.x;
+    pdl_wait();
+    for (int i = tid; i < N; i += nt) {
+        const unsigned char *p = (!INV || i < nl) ? static_cast<const unsigned char *>(r.a) + (long long)i * r.stride
+                                                  : static_cast<const unsigned char *>(r.b) + (long long)(i - nl) * r.stride;
+        A[i] = load_any(p);
+    }
+    __syncthreads();
+    recur::pass<NS, INV>(A, 0, 1, B, 0, 1, 1, N, W, tid, nt);
+    __syncthreads();
+    for (int i = tid; i < N; i += nt) {
+        unsigned char *p = (INV || i < nl) ? static_cast<unsigned char *>(r.c) + (long long)i * r.stride
+                                           : static_cast<unsigned char *>(r.h) + (long long)(i - nl) * r.stride;
+        store_any(p, B[i]);
     }
 }
 
@@ -592,24 +626,63 @@ cudaError_t launch_scatter_signals(const float *src, long long spitch, int N, vo
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather_calls(const CallRow *calls, int n_calls, int N, bool inverse, float *dst, long long dpitch,
-                                int h_off, cudaStream_t s)
+// The rows as a kernel parameter when they fit (and no device array is given).
+static bool call_rows_param(const CallRow *calls, const CallRow *host_calls, int n_calls, CallRowsParam &P)
+{
+    if (calls) return true;
+    if (!host_calls || n_calls > kCallRowsParam) return false;
+    for (int k = 0; k < n_calls; ++k) P.r[k] = host_calls[k];
+    return true;
+}
+
+cudaError_t launch_gather_calls(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, bool inverse,
+                                float *dst, long long dpitch, int h_off, cudaStream_t s)
 {
     if (n_calls <= 0 || N <= 0) return cudaSuccess;
     if (n_calls > 65535) return cudaErrorInvalidValue;
+    CallRowsParam P;
+    if (!call_rows_param(calls, host_calls, n_calls, P)) return cudaErrorInvalidValue;
     const dim3 grid(unsigned(std::min(ceil_div(N, 256), 64)), unsigned(n_calls));
-    gather_calls_kernel<<<grid, 256, 0, s>>>(calls, n_calls, N, inverse, dst, dpitch, h_off);
+    gather_calls_kernel<<<grid, 256, 0, s>>>(calls, P, n_calls, N, inverse, dst, dpitch, h_off);
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_calls(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
-                                 long long spitch, cudaStream_t s)
+cudaError_t launch_scatter_calls(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, bool inverse,
+                                 const float *src, long long spitch, cudaStream_t s)
 {
     if (n_calls <= 0 || N <= 0) return cudaSuccess;
     if (n_calls > 65535) return cudaErrorInvalidValue;
+    CallRowsParam P;
+    if (!call_rows_param(calls, host_calls, n_calls, P)) return cudaErrorInvalidValue;
     const dim3 grid(unsigned(std::min(ceil_div(N, 256), 64)), unsigned(n_calls));
-    scatter_calls_kernel<<<grid, 256, 0, s>>>(calls, n_calls, N, inverse, src, spitch);
+    scatter_calls_kernel<<<grid, 256, 0, s>>>(calls, P, n_calls, N, inverse, src, spitch);
     return cudaGetLastError();
+}
+
+cudaError_t launch_calls_1d(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, int wavelet,
+                            bool inverse, cudaStream_t s)
+{
+    if (n_calls <= 0 || N <= 0) return cudaSuccess;
+    if (N > kCalls1dMaxN || n_calls > 65535 * 32) return cudaErrorInvalidValue;
+    CallRowsParam P;
+    if (!call_rows_param(calls, host_calls, n_calls, P)) return cudaErrorInvalidValue;
+    static const cudaError_t configured = [] {
+        cudaError_t e = cudaSuccess;
+        for (auto k : {calls_1d_kernel<4, false>, calls_1d_kernel<4, true>, calls_1d_kernel<2, false>,
+                       calls_1d_kernel<2, true>})
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * kCalls1dMaxN);
+        return e;
+    }();
+    if (configured != cudaSuccess) return configured;
+    const Wavelet W = make_wavelet(wavelet, inverse);
+    const size_t smem = size_t(8) * N;
+    const dim3 g(static_cast<unsigned>(n_calls)), b(kCalls1dThreads);
+    if (wavelet == CDF97)
+        return inverse ? launch_pdl(calls_1d_kernel<4, true>, g, b, smem, s, calls, P, n_calls, N, W)
+                       : launch_pdl(calls_1d_kernel<4, false>, g, b, smem, s, calls, P, n_calls, N, W);
+    return inverse ? launch_pdl(calls_1d_kernel<2, true>, g, b, smem, s, calls, P, n_calls, N, W)
+                   : launch_pdl(calls_1d_kernel<2, false>, g, b, smem, s, calls, P, n_calls, N, W);
 }
 
 size_t sparse_tail_smem(int ox, int oy, int j0)

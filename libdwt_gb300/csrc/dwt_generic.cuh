@@ -53,12 +53,25 @@ struct CallRow {
     void *c, *h;
     long long stride;
 };
+// Up to kCallRowsParam calls travel as a kernel parameter (no descriptor
+// upload); larger batches read a device array.
+constexpr int kCallRowsParam = 64;
+struct CallRowsParam {
+    CallRow r[kCallRowsParam];
+};
 // The calls' signals (N samples each) into the rows of a compact frame
 // (inverse: L at the row's start, H from h_off), and the rows' results back.
-cudaError_t launch_gather_calls(const CallRow *calls, int n_calls, int N, bool inverse, float *dst, long long dpitch,
-                                int h_off, cudaStream_t s);
-cudaError_t launch_scatter_calls(const CallRow *calls, int n_calls, int N, bool inverse, const float *src,
-                                 long long spitch, cudaStream_t s);
+// `calls`: a device array of the n_calls rows, or null when n_calls <=
+// kCallRowsParam and `host_calls` holds them.
+cudaError_t launch_gather_calls(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, bool inverse,
+                                float *dst, long long dpitch, int h_off, cudaStream_t s);
+cudaError_t launch_scatter_calls(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, bool inverse,
+                                 const float *src, long long spitch, cudaStream_t s);
+// The calls transformed in one launch, one block per call, in shared memory
+// (N <= kCalls1dMaxN); `calls` / `host_calls` as above.
+constexpr int kCalls1dMaxN = 24576;
+cudaError_t launch_calls_1d(const CallRow *calls, const CallRow *host_calls, int n_calls, int N, int wavelet,
+                            bool inverse, cudaStream_t s);
 
 // The per-line levels of a sparse frame with zero padding in one CTA, the
 // frame of level j0 held in shared memory: forward levels j0 .. j1-1 or
