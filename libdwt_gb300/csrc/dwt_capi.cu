@@ -1561,10 +1561,10 @@ struct PendingCall {
     CallRow row;
     int rc;
     bool done;
+    std::condition_variable cv;  // the call's thread waits here (done, or asked to lead)
 };
 
 static std::mutex g_comb_mu;
-static std::condition_variable g_comb_cv;
 static std::vector<PendingCall *> g_comb_pending;
 static int g_comb_running = 0;  // batches in flight
 
@@ -1729,11 +1729,16 @@ static int run_1d_combined(PendingCall &me)
             lk.unlock();
             run_combined(batch);
             lk.lock();
-            for (PendingCall *q : batch) q->done = true;
             --g_comb_running;
-            g_comb_cv.notify_all();
+            // wake exactly the calls of the batch, and one queued call to
+            // lead the next batch (no herd of waiters on one variable)
+            for (PendingCall *q : batch) {
+                q->done = true;
+                if (q != &me) q->cv.notify_one();
+            }
+            if (!g_comb_pending.empty()) g_comb_pending.front()->cv.notify_one();
         } else {
-            g_comb_cv.wait(lk);
+            me.cv.wait(lk);
         }
     }
     return me.rc;
@@ -1761,7 +1766,7 @@ int run_1d(int wavelet, bool inverse, const float *a, const float *b, float *c_l
         const bool reach = (!inverse || nh == 0 || b) && (inverse || nh == 0 || h_out) &&
                            kernel_reaches_all(a, {c_l, inverse && nh ? b : nullptr, !inverse && nh ? h_out : nullptr});
         if (reach) {
-            PendingCall me{wavelet, inverse, N, CallRow{a, b, c_l, h_out, stride}, DWT_GPU_OK, false};
+            PendingCall me{wavelet, inverse, N, CallRow{a, b, c_l, h_out, stride}, DWT_GPU_OK, false, {}};
             return set_error(run_1d_combined(me));
         }
     }
