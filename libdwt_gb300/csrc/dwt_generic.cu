@@ -342,7 +342,8 @@ __global__ void scatter_calls_kernel(const CallRow *calls, const __grid_constant
 // shared memory, lifted there as per-thread windows of one line
 // (dwt_recur.cuh), and stored back at the call's destinations (forward: L
 // at c, H at h; inverse: N samples at c), all `stride` bytes apart.
-constexpr int kCalls1dThreads = 256;
+constexpr int kCalls1dThreads = 512;
+constexpr int kCalls1dUnroll = 8;  // loads (stores) in flight per thread
 
 template <int NS, bool INV>
 __global__ void __launch_bounds__(kCalls1dThreads) calls_1d_kernel(const CallRow *calls,
@@ -355,19 +356,35 @@ __global__ void __launch_bounds__(kCalls1dThreads) calls_1d_kernel(const CallRow
     const CallRow r = calls ? calls[k] : P.r[k];
     float *A = sm1, *B = sm1 + N;
     const int nl = (N + 1) / 2, tid = threadIdx.x, nt = blockDim.x;
+    const unsigned char *a = static_cast<const unsigned char *>(r.a), *b = static_cast<const unsigned char *>(r.b);
+    unsigned char *c = static_cast<unsigned char *>(r.c), *h = static_cast<unsigned char *>(r.h);
+    const long long st = r.stride;
+    // sample i of the source / destination (forward: N at a / L at c, H at
+    // h; inverse: L at a, H at b / N at c)
+    auto src = [&](int i) { return (!INV || i < nl) ? a + (long long)i * st : b + (long long)(i - nl) * st; };
+    auto dst = [&](int i) { return (INV || i < nl) ? c + (long long)i * st : h + (long long)(i - nl) * st; };
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                           reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(h) | uintptr_t(st)) & 3) == 0;
     pdl_wait();
-    for (int i = tid; i < N; i += nt) {
-        const unsigned char *p = (!INV || i < nl) ? static_cast<const unsigned char *>(r.a) + (long long)i * r.stride
-                                                  : static_cast<const unsigned char *>(r.b) + (long long)(i - nl) * r.stride;
-        A[i] = load_any(p);
+    for (int i0 = tid; i0 < N; i0 += kCalls1dUnroll * nt) {
+        float v[kCalls1dUnroll];
+#pragma unroll
+        for (int u = 0; u < kCalls1dUnroll; ++u) {
+            const int i = i0 + u * nt;
+            if (i < N) v[u] = aligned ? __ldg(reinterpret_cast<const float *>(src(i))) : load_any(src(i));
+        }
+#pragma unroll
+        for (int u = 0; u < kCalls1dUnroll; ++u)
+            if (i0 + u * nt < N) A[i0 + u * nt] = v[u];
     }
     __syncthreads();
     recur::pass<NS, INV>(A, 0, 1, B, 0, 1, 1, N, W, tid, nt);
     __syncthreads();
     for (int i = tid; i < N; i += nt) {
-        unsigned char *p = (INV || i < nl) ? static_cast<unsigned char *>(r.c) + (long long)i * r.stride
-                                           : static_cast<unsigned char *>(r.h) + (long long)(i - nl) * r.stride;
-        store_any(p, B[i]);
+        if (aligned)
+            *reinterpret_cast<float *>(dst(i)) = B[i];
+        else
+            store_any(dst(i), B[i]);
     }
 }
 
