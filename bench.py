@@ -325,6 +325,7 @@ def main():
                     help="run one secondary configuration alone and print its figures "
                          "(for profiler captures)")
     ap.add_argument("--c4-groups", type=int, default=8192, help="signal groups of C4 (8 signals each)")
+    ap.add_argument("--c2-images", type=int, default=4096, help="images of C2 (a smaller batch for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     global W, H, J, WORKLOAD, SERVE_SECONDS
@@ -350,7 +351,7 @@ def main():
         if args.only == "c4":
             res = run_signals_extra(D, torch, checks, groups=args.c4_groups)
         elif args.only == "c2":
-            res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks)
+            res = run_batch_extra(D, torch, stream, stream.cuda_stream, checks, n_images=args.c2_images)
         elif args.only == "dropin":
             res = run_dropin_extra(D, torch, torch.from_numpy(synth_image()).cuda(), args.dropin_reps)
         elif args.only == "dropin-dense":

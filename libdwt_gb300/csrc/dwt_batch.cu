@@ -255,6 +255,17 @@ void release_plan(dwt_gpu_batch *b)
     b->arena = nullptr;
 }
 
+// Whether the items of a phase are grouped by kernel variant (default on;
+// DWT_GPU_BATCH_GROUP_VARIANTS=0 keeps the image order).
+static bool sort_phases_by_variant()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_BATCH_GROUP_VARIANTS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 // Builds descriptors, items, scratch and the graph for the current params.
 int build_plan(dwt_gpu_batch *b)
 {
@@ -275,6 +286,15 @@ int build_plan(dwt_gpu_batch *b)
         scratch_off[i] = arena_floats;
         arena_floats += align_up_ll((long long)sf, 64);
     }
+    // within a phase, the items of one (wavelet, direction) together: the
+    // warps of an SM then mostly run one kernel variant at a time instead of
+    // evicting each other's code from the instruction cache (the order within
+    // a phase does not matter to the dependencies, which are on earlier phases)
+    auto variant = [&](const BatchItem &it) { return imgs[it.image].wavelet * 2 + (imgs[it.image].inverse ? 1 : 0); };
+    if (sort_phases_by_variant())
+        for (auto &v : by_phase)
+            std::stable_sort(v.begin(), v.end(),
+                             [&](const BatchItem &x, const BatchItem &y) { return variant(x) < variant(y); });
     std::vector<BatchItem> items;
     for (auto &v : by_phase) items.insert(items.end(), v.begin(), v.end());
     b->n_items = int(items.size());
