@@ -255,17 +255,6 @@ void release_plan(dwt_gpu_batch *b)
     b->arena = nullptr;
 }
 
-// Whether the items of a phase are grouped by kernel variant (default on;
-// DWT_GPU_BATCH_GROUP_VARIANTS=0 keeps the image order).
-static bool sort_phases_by_variant()
-{
-    static const bool on = [] {
-        const char *v = getenv("DWT_GPU_BATCH_GROUP_VARIANTS");
-        return !(v && v[0] == '0');
-    }();
-    return on;
-}
-
 // Builds descriptors, items, scratch and the graph for the current params.
 int build_plan(dwt_gpu_batch *b)
 {
@@ -288,13 +277,8 @@ int build_plan(dwt_gpu_batch *b)
     }
     // within a phase, the items of one (wavelet, direction) together: the
     // warps of an SM then mostly run one kernel variant at a time instead of
-    // evicting each other's code from the instruction cache (the order within
-    // a phase does not matter to the dependencies, which are on earlier phases)
-    auto variant = [&](const BatchItem &it) { return imgs[it.image].wavelet * 2 + (imgs[it.image].inverse ? 1 : 0); };
-    if (sort_phases_by_variant())
-        for (auto &v : by_phase)
-            std::stable_sort(v.begin(), v.end(),
-                             [&](const BatchItem &x, const BatchItem &y) { return variant(x) < variant(y); });
+    // evicting each other's code from the instruction cache
+    group_items_by_variant(by_phase, imgs);
     std::vector<BatchItem> items;
     for (auto &v : by_phase) items.insert(items.end(), v.begin(), v.end());
     b->n_items = int(items.size());
@@ -341,6 +325,27 @@ int build_plan(dwt_gpu_batch *b)
 }  // namespace
 
 namespace dwt {
+
+// Whether the items of a phase are grouped by kernel variant (default on;
+// DWT_GPU_BATCH_GROUP_VARIANTS=0 keeps the image order).
+static bool sort_phases_by_variant()
+{
+    static const bool on = [] {
+        const char *v = getenv("DWT_GPU_BATCH_GROUP_VARIANTS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+void group_items_by_variant(std::vector<std::vector<BatchItem>> &by_phase, const std::vector<BatchImage> &imgs)
+{
+    if (!sort_phases_by_variant()) return;
+    auto variant = [&](const BatchItem &it) { return imgs[it.image].wavelet * 2 + (imgs[it.image].inverse ? 1 : 0); };
+    for (auto &v : by_phase)
+        std::stable_sort(v.begin(), v.end(),
+                         [&](const BatchItem &x, const BatchItem &y) { return variant(x) < variant(y); });
+}
+
 
 size_t plan_image(BatchImage &I, const dwt_gpu_batch_image &u, const dwt_gpu_batch_params &P, int i,
                   std::vector<std::vector<BatchItem>> &by_phase)

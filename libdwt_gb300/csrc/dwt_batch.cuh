@@ -45,6 +45,12 @@ size_t plan_image(BatchImage &I, const dwt_gpu_batch_image &u, const dwt_gpu_bat
 // Points the descriptor's two LL scratch frames into `scratch`.
 void set_image_scratch(BatchImage &I, float *scratch);
 
+// Orders the items of every phase by kernel variant (wavelet, direction),
+// keeping the image order within a variant, so that the warps of an SM
+// mostly run one variant's code at a time (DWT_GPU_BATCH_GROUP_VARIANTS=0:
+// no change).  The dependencies are on earlier phases only.
+void group_items_by_variant(std::vector<std::vector<BatchItem>> &by_phase, const std::vector<BatchImage> &imgs);
+
 // Shared memory of the batched kernel per CTA.
 int batch_smem_bytes();
 

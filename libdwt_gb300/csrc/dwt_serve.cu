@@ -150,6 +150,7 @@ void launch_flight(dwt_gpu_server *S, Flight &f)
         else
             dwt::set_image_scratch(imgs.back(), static_cast<float *>(q.scratch));
     }
+    dwt::group_items_by_variant(by_phase, imgs);
     size_t n_items = 0;
     for (auto &v : by_phase) n_items += v.size();
     const size_t img_b = sizeof(BatchImage) * imgs.size();
