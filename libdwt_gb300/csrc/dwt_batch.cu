@@ -196,8 +196,7 @@ batch_kernel(const BatchImage *__restrict__ imgs, const BatchItem *__restrict__ 
         // warp's writes ordered before it by the warp barrier)
         __syncwarp();
         if (lane == 0) {
-            __threadfence();
-            atomicAdd(done + it.image * kPhases + it.phase, 1);
+            red_release_add(done + it.image * kPhases + it.phase, 1);
         }
     }
 }

@@ -239,6 +239,14 @@ __device__ __forceinline__ int ld_acquire(const int *p)
     return v;
 }
 
+// Release increment of a counter another warp acquires: the writes this
+// thread has made (and those of the warp ordered before it by a warp
+// barrier) are visible to an acquirer that sees the increment.
+__device__ __forceinline__ void red_release_add(int *p, int v)
+{
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ void fence_proxy_async_global()
 {
     asm volatile("fence.proxy.async.global;" ::: "memory");
