@@ -104,3 +104,23 @@ def test_per_signal_calls_from_16_threads(env, where):
         torch.cuda.synchronize()
         got_i = dev.cpu().numpy()
     assert np.array_equal(got_i.view(np.uint32), ref_i.view(np.uint32)), "inverse differs"
+
+
+@pytest.mark.parametrize("n", [24576, 24577, 30001])
+def test_long_signals_from_threads(env, n):
+    """Signals longer than the one-launch kernel's shared-memory limit (24576
+    samples) take the gather / level / scatter launches: the same bits."""
+    L, torch = env
+    rng = np.random.default_rng(n)
+    groups, lanes = 2, LANES
+    bank = rng.uniform(-50, 50, size=(groups, n + 3, lanes)).astype(np.float32)
+    calls = [(s, n, ("cdf97", "cdf53")[s % 2]) for s in range(groups * lanes)]
+    ref_f = _oracle(bank, calls, n, "f")
+    ref_i = _oracle(ref_f, calls, n, "i")
+    dev = torch.from_numpy(bank.copy()).cuda()
+    _run_threads(L, dev.data_ptr(), calls, n, "f", threads=4)
+    torch.cuda.synchronize()
+    assert np.array_equal(dev.cpu().numpy().view(np.uint32), ref_f.view(np.uint32)), "forward differs"
+    _run_threads(L, dev.data_ptr(), calls, n, "i", threads=4)
+    torch.cuda.synchronize()
+    assert np.array_equal(dev.cpu().numpy().view(np.uint32), ref_i.view(np.uint32)), "inverse differs"
