@@ -53,7 +53,7 @@ __global__ void order_wait_timeout_kernel(LevelDesc D, uint32_t limit, int *err)
     units::order_wait(D, false, 2, 0, threadIdx.x & 31, err, limit);
 }
 
-template <int NS, bool INV, bool ORD>
+template <int NS, bool INV, bool ORD, bool VST = true>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, ORD ? 5 : 0)
 level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant__ LevelMaps M)
 {
@@ -101,7 +101,8 @@ level_kernel(const LevelDesc D, const Wavelet W, int *err, const __grid_constant
             const int q = u / D.n_strips;
             const int strip = u % D.n_strips, seg = D.seg_base + (D.reverse ? D.n_segs - 1 - q : q);
             int unused = 0;
-            if (!units::run_unit<NS, INV>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp, unused))
+            if (!units::run_unit<NS, INV, false, VST>(D, W, strip, seg, ring, bars, tick, lane, err, fast_launch, mp,
+                                                      unused))
                 break;
         }
     }
@@ -174,12 +175,12 @@ bool encode_inverse_maps(const LevelDesc &d, LevelMaps &M, int box_w, int &dx, i
     return ok;
 }
 
-template <int NS, bool INV, bool ORD>
+template <int NS, bool INV, bool ORD, bool VST = true>
 cudaError_t launch_o(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
 {
     // once per instantiation, safe from several host threads
     static const cudaError_t configured =
-        cudaFuncSetAttribute(level_kernel<NS, INV, ORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+        cudaFuncSetAttribute(level_kernel<NS, INV, ORD, VST>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (configured != cudaSuccess) return configured;
     const int units = d.n_strips * d.n_segs;
     const int grid = ceil_div(units, kWarpsPerCta);
@@ -190,14 +191,29 @@ cudaError_t launch_o(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, 
     dd.tmap = (INV && tensor_copies_enabled() && encode_inverse_maps(d, M, kBandRowF, dx, dy)) ? 1 : 0;
     dd.map_dx = dx;
     dd.map_dy = dy;
-    return launch_pdl(level_kernel<NS, INV, ORD>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd, W,
-                      err, M);
+    return launch_pdl(level_kernel<NS, INV, ORD, VST>, dim3(grid), dim3(kWarpsPerCta * 32), kSmemBytes, stream, dd,
+                      W, err, M);
+}
+
+// Whether the forward level's band rows take 8-byte stores (the device-side
+// check of units::fast_ok, on the host).
+bool forward_stores_aligned(const LevelDesc &d)
+{
+    for (int k = 0; k < 4; ++k)
+        if ((reinterpret_cast<uintptr_t>(d.out[k]) & 7) != 0 || (d.out_pitch[k] & 1) != 0) return false;
+    return true;
 }
 
 template <int NS, bool INV>
 cudaError_t launch_t(const LevelDesc &d, const Wavelet &W, cudaStream_t stream, int *err)
 {
-    return d.order ? launch_o<NS, INV, true>(d, W, stream, err) : launch_o<NS, INV, false>(d, W, stream, err);
+    if (d.order) return launch_o<NS, INV, true>(d, W, stream, err);
+    // forward levels whose bands cannot take 8-byte stores: a kernel whose
+    // interior strips keep the fast loads and store one by one
+    if constexpr (!INV)
+        if (!d.rows_only && d.h > 1 && !forward_stores_aligned(d))
+            return launch_o<NS, INV, false, false>(d, W, stream, err);
+    return launch_o<NS, INV, false>(d, W, stream, err);
 }
 
 }  // namespace

@@ -377,7 +377,7 @@ __device__ __forceinline__ void unit_span(const LevelDesc &D, int seg, int &k0, 
 // path for strips touching the left or right border (mirrored columns,
 // partial lanes) or unaligned outputs.  The rows are staged from column B
 // on, `win` columns wide, `slot_f` floats per row slot.
-template <int NS, bool EDGE, class Pipe, bool ORD = false>
+template <int NS, bool EDGE, class Pipe, bool ORD = false, bool VST = true>
 __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, const Pipe &pipe, int B,
                              int win, int slot_f, uint32_t &tick, int lane, int *err, int &next)
 {
@@ -513,11 +513,24 @@ __device__ bool forward_unit(const LevelDesc &D, const Wavelet &W, int strip, in
                         if (vH1) pHH[1] = f2hi(HO);
                     }
                 } else if (lane_ok) {
-                    *reinterpret_cast<f2 *>(pLL) = LE;
-                    *reinterpret_cast<f2 *>(pHL) = LO;
-                    if (p <= last_h) {
-                        *reinterpret_cast<f2 *>(pLH) = HE;
-                        *reinterpret_cast<f2 *>(pHH) = HO;
+                    if (VST) {
+                        *reinterpret_cast<f2 *>(pLL) = LE;
+                        *reinterpret_cast<f2 *>(pHL) = LO;
+                        if (p <= last_h) {
+                            *reinterpret_cast<f2 *>(pLH) = HE;
+                            *reinterpret_cast<f2 *>(pHH) = HO;
+                        }
+                    } else {  // band rows not 8-byte aligned (an odd pitch): the same samples one by one
+                        pLL[0] = f2lo(LE);
+                        pLL[1] = f2hi(LE);
+                        pHL[0] = f2lo(LO);
+                        pHL[1] = f2hi(LO);
+                        if (p <= last_h) {
+                            pLH[0] = f2lo(HE);
+                            pLH[1] = f2hi(HE);
+                            pHH[0] = f2lo(HO);
+                            pHH[1] = f2hi(HO);
+                        }
                     }
                 }
                 pLL += D.out_pitch[0];
@@ -902,7 +915,7 @@ __device__ __forceinline__ bool fast_ok(const LevelDesc &D)
 
 // Runs one unit (strip, seg) of the level described by D on a warp's
 // private ring.
-template <int NS, bool INV, bool ORD = false>
+template <int NS, bool INV, bool ORD = false, bool VST = true>
 __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, int strip, int seg, float *ring,
                                          uint64_t *bars, uint32_t &tick, int lane, int *err, bool fast_launch,
                                          const LevelMaps *maps, int &next)
@@ -911,8 +924,18 @@ __device__ __forceinline__ bool run_unit(const LevelDesc &D, const Wavelet &W, i
         return INV ? inverse_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err)
                    : forward_rows_unit<NS>(D, W, strip, seg, ring, bars, tick, lane, err);
     const int b = strip * kStripOut - 4;
-    const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
     const WarpPipe pipe{ring, bars};
+    if constexpr (!INV && !VST) {
+        // a forward launch whose bands are not 8-byte aligned (an odd pitch):
+        // the alignment only concerns the stores (the rows come from the
+        // ring), so interior strips keep the fast loads and store one by one
+        if (b < 0 || b + kStripIn + 2 > D.w)
+            return forward_unit<NS, true, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane, err,
+                                                         next);
+        return forward_unit<NS, false, WarpPipe, ORD, false>(D, W, strip, seg, pipe, b, kStripIn, kSlotF, tick, lane,
+                                                             err, next);
+    }
+    const bool edge = !fast_launch || b < 0 || b + kStripIn + 2 > D.w;
     if (INV)
         return edge ? inverse_unit<NS, true, WarpPipe, ORD>(D, W, strip, seg, pipe, b, kStripIn / 2, maps, tick, lane,
                                                             err, next)
