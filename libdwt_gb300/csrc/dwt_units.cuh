@@ -707,7 +707,6 @@ __device__ bool inverse_unit(const LevelDesc &D, const Wavelet &W, int strip, in
     const int bq = b >> 1;  // band column of lane 0's first value
     const int bqB = B >> 1;  // band column of the staged window's start
     const int Lw = (w + 1) >> 1, Hw = w >> 1;
-    const int hs = (h + 1) >> 1;
     int k0, total, iters;
     unit_span<NS>(D, seg, k0, total, iters);
     const int m0 = k0 - LAT;
